@@ -1,0 +1,185 @@
+"""ctypes binding of the engine library (lib/libacoustic3d.so, include/acoustic3d.h).
+
+There is no fallback: if the library is missing or cannot be loaded, every entry
+point raises.  Build it with ``python acoustic3d-fd_gb300/build.py``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(HERE, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libacoustic3d.so")
+LEGACY_LIBS = {"2order": "acoustic2order.so", "1order": "acoustic1order.so",
+               "vti": "acoustic1vti.so", "tti": "acoustic1tti.so"}
+
+ORDER2, ISO, VTI, TTI = 0, 1, 2, 3
+FP32, BF16, FP16, FP64 = 0, 1, 2, 3
+PHYSICS = {"2o": ORDER2, "iso": ISO, "vti": VTI, "tti": TTI}
+MODEL_NAMES = ("vel", "rho", "eps", "del", "theta", "phi")
+READS = {ORDER2: ("vel",), ISO: ("vel", "rho"), VTI: ("vel", "rho", "eps", "del"),
+         TTI: ("vel", "eps", "del", "theta", "phi")}
+
+A3D_OK, A3D_E_ARG, A3D_E_IO, A3D_E_CUDA, A3D_E_NOMEM, A3D_E_KERNEL, A3D_E_UNSUPPORTED = range(7)
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("physics", ctypes.c_int),
+                ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("dx", ctypes.c_float), ("dy", ctypes.c_float), ("dz", ctypes.c_float),
+                ("nt", ctypes.c_int), ("dt", ctypes.c_float), ("fm", ctypes.c_float),
+                ("wtype", ctypes.c_int), ("npml", ctypes.c_int), ("rec_z", ctypes.c_int),
+                ("mute", ctypes.c_int), ("storage", ctypes.c_int), ("tile_x", ctypes.c_int)]
+
+
+class ShotPos(ctypes.Structure):
+    _fields_ = [("sx", ctypes.c_int), ("sy", ctypes.c_int), ("sz", ctypes.c_int)]
+
+
+class A3DError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"acoustic3d status {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+_FP = ctypes.POINTER(ctypes.c_float)
+
+
+def lib() -> ctypes.CDLL:
+    """Load the engine library (raises if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run acoustic3d-fd_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        vp = ctypes.c_void_p
+        L.a3d_engine_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(Config)] + [_FP] * 6 + [ctypes.c_int]
+        L.a3d_engine_create.restype = ctypes.c_int
+        L.a3d_engine_destroy.argtypes = [vp]
+        L.a3d_engine_destroy.restype = ctypes.c_int
+        L.a3d_engine_run.argtypes = [vp, ctypes.POINTER(ShotPos), _FP, ctypes.c_int, ctypes.c_int, _FP,
+                                     ctypes.POINTER(ctypes.c_double)]
+        L.a3d_engine_run.restype = ctypes.c_int
+        L.a3d_engine_run_device.argtypes = [vp, ctypes.POINTER(ShotPos), vp, ctypes.POINTER(ctypes.c_double)]
+        L.a3d_engine_run_device.restype = ctypes.c_int
+        L.a3d_engine_record_device.argtypes = [vp]
+        L.a3d_engine_record_device.restype = vp
+        L.a3d_engine_device_bytes.argtypes = [vp]
+        L.a3d_engine_device_bytes.restype = ctypes.c_size_t
+        L.a3d_forward_host.argtypes = [ctypes.POINTER(Config)] + [_FP] * 6 + [ctypes.POINTER(ShotPos),
+                                                                               ctypes.c_int, _FP, ctypes.c_int]
+        L.a3d_forward_host.restype = ctypes.c_int
+        L.a3d_last_error.argtypes = []
+        L.a3d_last_error.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().a3d_last_error().decode(errors="replace")
+
+
+def _check(rc):
+    if rc != A3D_OK:
+        raise A3DError(rc, last_error())
+
+
+def _fptr(a):
+    if a is None:
+        return ctypes.cast(None, _FP)
+    return a.ctypes.data_as(_FP)
+
+
+def make_config(physics, nx, ny, nz, dx=10.0, dy=10.0, dz=10.0, nt=100, dt=1e-3, fm=20.0, wtype=1,
+                npml=0, rec_z=-1, mute=False, storage=FP32, tile_x=0) -> Config:
+    if isinstance(physics, str):
+        physics = PHYSICS[physics]
+    return Config(physics, nx, ny, nz, dx, dy, dz, nt, dt, fm, wtype, npml, rec_z, int(mute), storage, tile_x)
+
+
+class Engine:
+    """A model resident on the GPU; run shots against it."""
+
+    def __init__(self, cfg: Config, models: dict, device: int = 0):
+        self.cfg = cfg
+        n = cfg.nx * cfg.ny * cfg.nz
+        self._keep = {}
+        ptrs = []
+        for name in MODEL_NAMES:
+            a = models.get(name)
+            if a is not None and name in READS[cfg.physics]:
+                a = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+                if a.size != n:
+                    raise ValueError(f"model {name} has {a.size} values, expected {n}")
+                self._keep[name] = a
+            else:
+                a = None
+            ptrs.append(_fptr(a))
+        h = ctypes.c_void_p()
+        _check(lib().a3d_engine_create(ctypes.byref(h), ctypes.byref(cfg), *ptrs, device))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().a3d_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, sx, sy, sz, snap_every=0, snap_skip0=False, with_time=False):
+        """Run one shot; returns record[ny, nx, nt] (and snapshots, device ms)."""
+        c = self.cfg
+        rec = np.zeros((c.ny, c.nx, c.nt), dtype=np.float32)
+        nsnap = 0
+        if snap_every > 0:
+            nsnap = sum(1 for it in range(c.nt) if it % snap_every == 0 and not (snap_skip0 and it == 0))
+        snaps = np.zeros((max(nsnap, 1), c.ny, c.nx, c.nz), np.float32) if nsnap else None
+        ms = ctypes.c_double(0.0)
+        _check(lib().a3d_engine_run(self.h, ctypes.byref(ShotPos(sx, sy, sz)), _fptr(rec), snap_every,
+                                    int(snap_skip0), _fptr(snaps), ctypes.byref(ms)))
+        out = (rec,)
+        if snap_every > 0:
+            out += (snaps,)
+        if with_time:
+            out += (ms.value,)
+        return out[0] if len(out) == 1 else out
+
+    def run_device(self, sx, sy, sz, rec_dev_ptr=None) -> float:
+        """Run one shot leaving the record on the device; returns device ms."""
+        ms = ctypes.c_double(0.0)
+        _check(lib().a3d_engine_run_device(self.h, ctypes.byref(ShotPos(sx, sy, sz)),
+                                           ctypes.c_void_p(rec_dev_ptr), ctypes.byref(ms)))
+        return ms.value
+
+    def record_device_ptr(self) -> int:
+        return lib().a3d_engine_record_device(self.h)
+
+    def device_bytes(self) -> int:
+        return lib().a3d_engine_device_bytes(self.h)
+
+
+def forward_host(cfg: Config, models: dict, shots, device: int = 0):
+    """One call from host buffers: upload, run every shot, copy the records back."""
+    n = cfg.nx * cfg.ny * cfg.nz
+    ptrs, keep = [], []
+    for name in MODEL_NAMES:
+        a = models.get(name)
+        if a is not None and name in READS[cfg.physics]:
+            a = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+            assert a.size == n
+            keep.append(a)
+            ptrs.append(_fptr(a))
+        else:
+            ptrs.append(_fptr(None))
+    arr = (ShotPos * len(shots))(*[ShotPos(*s) for s in shots])
+    recs = np.zeros((len(shots), cfg.ny, cfg.nx, cfg.nt), np.float32)
+    _check(lib().a3d_forward_host(ctypes.byref(cfg), *ptrs, arr, len(shots), _fptr(recs), device))
+    return recs

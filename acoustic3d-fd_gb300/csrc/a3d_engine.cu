@@ -1,0 +1,558 @@
+// a3d_engine.cu — engine object: model upload, tensor maps, the time loops of
+// the four physics, and the in-memory C API (a3d_*).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "a3d_engine.h"
+
+namespace a3d {
+
+static thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    fprintf(stderr, "acoustic3d: %s\n", buf);
+    return code;
+}
+void clear_error() { g_err.clear(); }
+
+#define CUDA_TRY(x)                                                                    \
+    do {                                                                               \
+        cudaError_t e_ = (x);                                                          \
+        if (e_ != cudaSuccess)                                                         \
+            return fail(A3D_E_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_));      \
+    } while (0)
+
+static int g_sms = 0;
+int occ_grid(int occ, long long W) {
+    long long g = (long long)(g_sms > 0 ? g_sms : 148) * (occ > 0 ? occ : 1);
+    long long cap = W / 24;
+    if (cap < 1) cap = 1;
+    return (int)(g < cap ? g : cap);
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// 3-D map over a padded field: dims (nnz, nnx, nny), row stride ldz elements
+static int make_map(CUtensorMap *m, const void *base, bool f64, const Grid &g, int box0, int box1) {
+    auto enc = encode_fn();
+    if (!enc) return fail(A3D_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    const size_t es = f64 ? 8 : 4;
+    cuuint64_t dims[3] = {(cuuint64_t)g.nnz, (cuuint64_t)g.nnx, (cuuint64_t)g.nny};
+    cuuint64_t strides[2] = {(cuuint64_t)(g.ldz * es), (cuuint64_t)((size_t)g.ldz * g.nnx * es)};
+    cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(m, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                     const_cast<void *>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(A3D_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return A3D_OK;
+}
+
+static int box_dims(int box, int tx, int &b0, int &b1) {
+    b0 = (box == BOX_HZ || box == BOX_H) ? 40 : 32;
+    b1 = (box == BOX_HX || box == BOX_H) ? tx + 8 : tx;
+    return 0;
+}
+
+// crop of the model window of a padded field into dense float [ny][nx][nz]
+template <class S>
+__global__ void crop_window(const S *f, float *out, int nx, int ny, int nz, int pad, int ldz,
+                            int nnx) {
+    const size_t n = (size_t)nx * ny * nz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(i % nz);
+        const size_t r = i / nz;
+        const int ix = (int)(r % nx), iy = (int)(r / nx);
+        out[i] = (float)f[(size_t)(iz + pad) + (size_t)ldz * ((size_t)(ix + pad) + (size_t)nnx * (iy + pad))];
+    }
+}
+
+}  // namespace a3d
+
+using namespace a3d;
+
+a3d_engine::~a3d_engine() {
+    if (st) cudaStreamSynchronize(st);
+    for (void *p : allocs) cudaFree(p);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (st) cudaStreamDestroy(st);
+}
+
+void *a3d_engine::dalloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, bytes) != cudaSuccess) { cudaFree(p); return nullptr; }
+    allocs.push_back(p);
+    dev_bytes += bytes;
+    return p;
+}
+
+static int upload_model(a3d_engine *e, const float *m, float **dst, std::vector<float> &tmp) {
+    const Grid &g = e->g;
+    pad_model(m, g, tmp.data());
+    *dst = (float *)e->dalloc(g.elems() * 4);
+    if (!*dst) return fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", g.elems() * 4);
+    CUDA_TRY(cudaMemcpy(*dst, tmp.data(), g.elems() * 4, cudaMemcpyHostToDevice));
+    return A3D_OK;
+}
+
+static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const float *eps,
+                        const float *del, const float *theta, const float *phi) {
+    const a3d_config &c = e->cfg;
+    const Grid &g = e->g;
+    std::vector<float> tmp(g.elems());
+    const size_t fb = g.elems() * e->esz;
+    auto field = [&](void **p) -> int {
+        *p = e->dalloc(fb);
+        return *p ? A3D_OK : fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", fb);
+    };
+    int rc;
+    e->rec = (float *)e->dalloc((size_t)c.nt * c.nx * c.ny * 4);
+    e->d_mute = (int *)e->dalloc((size_t)c.nx * c.ny * 4);
+    e->snap_dev = (float *)e->dalloc((size_t)c.nx * c.ny * c.nz * 4);
+    if (!e->rec || !e->d_mute || !e->snap_dev) return fail(A3D_E_NOMEM, "record allocation failed");
+
+    if (c.physics == A3D_2ORDER) {
+        // vv = (v dt)^2 on the padded grid (Toa_3dfd_cuda.cu:300-347)
+        pad_model(vel, g, tmp.data());
+        for (size_t i = 0; i < tmp.size(); ++i) {
+            const float t = tmp[i] * c.dt;
+            tmp[i] = t * t;
+        }
+        e->vv = (float *)e->dalloc(g.elems() * 4);
+        if (!e->vv) return fail(A3D_E_NOMEM, "device allocation failed");
+        CUDA_TRY(cudaMemcpy(e->vv, tmp.data(), g.elems() * 4, cudaMemcpyHostToDevice));
+        e->v_mute = (size_t)c.nx * c.ny * c.nz > 1 ? vel[1] : vel[0];  // 2O:403
+        if ((rc = field(&e->X)) || (rc = field(&e->Y))) return rc;
+        // sponge factors per axis
+        std::vector<float> hl;
+        float2 **dst[3] = {&e->fz, &e->fx, &e->fy};
+        const int n3[3] = {c.nz, c.nx, c.ny}, nn3[3] = {g.nnz, g.nnx, g.nny};
+        for (int a = 0; a < 3; ++a) {
+            hl.assign(2 * (size_t)nn3[a], 0.0f);
+            sponge_factors(n3[a], e->npml, hl.data());
+            *dst[a] = (float2 *)e->dalloc(hl.size() * 4);
+            if (!*dst[a]) return fail(A3D_E_NOMEM, "device allocation failed");
+            CUDA_TRY(cudaMemcpy(*dst[a], hl.data(), hl.size() * 4, cudaMemcpyHostToDevice));
+        }
+        e->w2o.resize(c.nt);
+        for (int it = 0; it < c.nt; ++it) e->w2o[it] = ricker2o(it, c.dt, c.fm);
+        const bool f64 = e->fp64;
+        void *buf[2] = {e->X, e->Y};
+        for (int b = 0; b < 2; ++b) {
+            if ((rc = make_map(&e->m2o_cur[b], buf[b], f64, g, 40, e->tx + 8))) return rc;
+            if ((rc = make_map(&e->m2o_prev[b], buf[b], f64, g, 32, e->tx))) return rc;
+        }
+        return make_map(&e->m2o_vv, e->vv, false, g, 32, e->tx);
+    }
+
+    // 1st-order engines
+    if ((rc = upload_model(e, vel, &e->vp, tmp))) return rc;
+    if (c.physics != A3D_TTI && (rc = upload_model(e, rho, &e->rho, tmp))) return rc;
+    if (c.physics != A3D_ISO) {
+        if ((rc = upload_model(e, eps, &e->eps, tmp))) return rc;
+        if ((rc = upload_model(e, del, &e->del, tmp))) return rc;
+    }
+    if (c.physics == A3D_TTI) {
+        // cos/sin of tilt and azimuth in float, as ..tti..:101-103 evaluates them
+        std::vector<float> ang(g.elems());
+        float **dst[4] = {&e->tct, &e->tst, &e->tcp, &e->tsp};
+        for (int k = 0; k < 4; ++k) {
+            pad_model(k < 2 ? theta : phi, g, ang.data());
+            for (size_t i = 0; i < ang.size(); ++i) tmp[i] = (k % 2 == 0) ? cosf(ang[i]) : sinf(ang[i]);
+            *dst[k] = (float *)e->dalloc(g.elems() * 4);
+            if (!*dst[k]) return fail(A3D_E_NOMEM, "device allocation failed");
+            CUDA_TRY(cudaMemcpy(*dst[k], tmp.data(), g.elems() * 4, cudaMemcpyHostToDevice));
+        }
+    }
+    // mute velocity: the padded model's element 1, i.e. model cell (0,0,0) (..iso..:340)
+    e->v_mute = vel[0];
+    if (c.physics != A3D_ISO) e->v_mute = vel[0] * sqrtf(1.0f + 2.0f * eps[0]);  // ..vti..:357
+    if ((rc = field(&e->u)) || (rc = field(&e->v)) || (rc = field(&e->w)) || (rc = field(&e->P)) ||
+        (rc = field(&e->px)) || (rc = field(&e->py)) || (rc = field(&e->pz)))
+        return rc;
+    if (c.physics != A3D_ISO) {
+        if ((rc = field(&e->Q)) || (rc = field(&e->qx)) || (rc = field(&e->qy)) || (rc = field(&e->qz)))
+            return rc;
+    }
+    // PML profiles (..iso..:193-195 and 263-291): d0 from the padded model's middle element
+    const size_t mid = ((size_t)g.nny * g.nnx * g.nnz) / 2;  // flat index in the reference's dense layout
+    const int miz = (int)(mid % g.nnz), mix = (int)((mid / g.nnz) % g.nnx), miy = (int)(mid / ((size_t)g.nnz * g.nnx));
+    float vmid;
+    {
+        int cz = std::min(std::max(miz - g.pad, 0), c.nz - 1), cx = std::min(std::max(mix - g.pad, 0), c.nx - 1),
+            cy = std::min(std::max(miy - g.pad, 0), c.ny - 1);
+        vmid = vel[cz + (size_t)c.nz * (cx + (size_t)c.nx * cy)];
+    }
+    const float d0 = pml_d0(vmid, e->npml, c.dx, c.dy, c.dz);
+    std::vector<float> pm(4 * (size_t)(g.nnx + g.nny + g.nnz));
+    float *q = pm.data();
+    const int n3[3] = {c.nx, c.ny, c.nz}, nn3[3] = {g.nnx, g.nny, g.nnz};
+    for (int a = 0; a < 3; ++a) {
+        pml_profile(c.dt, d0, n3[a], e->npml, q, q + nn3[a], q + 2 * nn3[a], q + 3 * nn3[a]);
+        q += 4 * nn3[a];
+    }
+    e->pml = (float *)e->dalloc(pm.size() * 4);
+    if (!e->pml) return fail(A3D_E_NOMEM, "device allocation failed");
+    CUDA_TRY(cudaMemcpy(e->pml, pm.data(), pm.size() * 4, cudaMemcpyHostToDevice));
+    {
+        float tb[2 * 226];
+        sv_taper_table(tb);
+        e->taper = (float2 *)e->dalloc(sizeof tb);
+        if (!e->taper) return fail(A3D_E_NOMEM, "device allocation failed");
+        CUDA_TRY(cudaMemcpy(e->taper, tb, sizeof tb, cudaMemcpyHostToDevice));
+    }
+    // injected amplitudes per step; t accumulates in float (..iso..:521)
+    e->amp0.resize(c.nt);
+    e->amp1.resize(c.nt);
+    e->inj.resize(c.nt);
+    const float tdelay = (float)(1.0 / (double)c.fm);
+    float t = c.dt;
+    for (int it = 0; it < c.nt; ++it, t += c.dt) {
+        const float src = wavelet1(c.physics == A3D_ISO ? c.wtype : 1, t, c.fm);
+        e->inj[it] = t <= 2.0f * tdelay;
+        if (c.physics == A3D_ISO) {
+            const float pfac = 10000.0f;  // ..iso..:407
+            e->amp0[it] = -pfac * src;
+            e->amp1[it] = pfac * src;
+        } else {
+            const float pfac = 10.0f;     // ..vti..:431, ..tti..:437
+            e->amp0[it] = pfac * src;
+            e->amp1[it] = pfac * src;
+        }
+    }
+    // tensor maps
+    const bool f64 = e->fp64;
+    const int tx = e->tx;
+    int b0, b1;
+    auto mk = [&](CUtensorMap *m, const void *p, bool isfield, int box) {
+        box_dims(box, tx, b0, b1);
+        return make_map(m, p, isfield && f64, g, b0, b1);
+    };
+    if (c.physics == A3D_ISO) {
+        e->nvel = 5;
+        if ((rc = mk(&e->mvel[0], e->P, true, BOX_H)) || (rc = mk(&e->mvel[1], e->u, true, BOX_CORE)) ||
+            (rc = mk(&e->mvel[2], e->v, true, BOX_CORE)) || (rc = mk(&e->mvel[3], e->w, true, BOX_CORE)) ||
+            (rc = mk(&e->mvel[4], e->rho, false, BOX_CORE)))
+            return rc;
+        e->nstr = 6;
+        if ((rc = mk(&e->mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&e->mstr[1], e->u, true, BOX_HX)) ||
+            (rc = mk(&e->mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&e->mstr[3], e->P, true, BOX_CORE)) ||
+            (rc = mk(&e->mstr[4], e->rho, false, BOX_CORE)) || (rc = mk(&e->mstr[5], e->vp, false, BOX_CORE)))
+            return rc;
+    } else if (c.physics == A3D_VTI) {
+        e->nvel = 6;
+        if ((rc = mk(&e->mvel[0], e->P, true, BOX_HX)) || (rc = mk(&e->mvel[1], e->Q, true, BOX_HZ)) ||
+            (rc = mk(&e->mvel[2], e->u, true, BOX_CORE)) || (rc = mk(&e->mvel[3], e->v, true, BOX_CORE)) ||
+            (rc = mk(&e->mvel[4], e->w, true, BOX_CORE)) || (rc = mk(&e->mvel[5], e->rho, false, BOX_CORE)))
+            return rc;
+        e->nstr = 9;
+        if ((rc = mk(&e->mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&e->mstr[1], e->u, true, BOX_HX)) ||
+            (rc = mk(&e->mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&e->mstr[3], e->P, true, BOX_CORE)) ||
+            (rc = mk(&e->mstr[4], e->Q, true, BOX_CORE)) || (rc = mk(&e->mstr[5], e->rho, false, BOX_CORE)) ||
+            (rc = mk(&e->mstr[6], e->vp, false, BOX_CORE)) || (rc = mk(&e->mstr[7], e->eps, false, BOX_CORE)) ||
+            (rc = mk(&e->mstr[8], e->del, false, BOX_CORE)))
+            return rc;
+    } else {
+        e->nvel = 9;
+        if ((rc = mk(&e->mvel[0], e->P, true, BOX_H)) || (rc = mk(&e->mvel[1], e->Q, true, BOX_H)) ||
+            (rc = mk(&e->mvel[2], e->u, true, BOX_CORE)) || (rc = mk(&e->mvel[3], e->v, true, BOX_CORE)) ||
+            (rc = mk(&e->mvel[4], e->w, true, BOX_CORE)) || (rc = mk(&e->mvel[5], e->tct, false, BOX_CORE)) ||
+            (rc = mk(&e->mvel[6], e->tst, false, BOX_CORE)) || (rc = mk(&e->mvel[7], e->tcp, false, BOX_CORE)) ||
+            (rc = mk(&e->mvel[8], e->tsp, false, BOX_CORE)))
+            return rc;
+        e->nstr = 12;
+        if ((rc = mk(&e->mstr[0], e->u, true, BOX_H)) || (rc = mk(&e->mstr[1], e->v, true, BOX_H)) ||
+            (rc = mk(&e->mstr[2], e->w, true, BOX_H)) || (rc = mk(&e->mstr[3], e->P, true, BOX_CORE)) ||
+            (rc = mk(&e->mstr[4], e->Q, true, BOX_CORE)) || (rc = mk(&e->mstr[5], e->vp, false, BOX_CORE)) ||
+            (rc = mk(&e->mstr[6], e->eps, false, BOX_CORE)) || (rc = mk(&e->mstr[7], e->del, false, BOX_CORE)) ||
+            (rc = mk(&e->mstr[8], e->tct, false, BOX_CORE)) || (rc = mk(&e->mstr[9], e->tst, false, BOX_CORE)) ||
+            (rc = mk(&e->mstr[10], e->tcp, false, BOX_CORE)) || (rc = mk(&e->mstr[11], e->tsp, false, BOX_CORE)))
+            return rc;
+    }
+    return A3D_OK;
+}
+
+static int check_kernel_error(a3d_engine *e) {
+    int herr = 0;
+    CUDA_TRY(cudaMemcpyAsync(&herr, e->d_err, sizeof(int), cudaMemcpyDeviceToHost, e->st));
+    CUDA_TRY(cudaStreamSynchronize(e->st));
+    if (herr)
+        return fail(A3D_E_KERNEL, "a kernel gave up a bounded wait (code %d); results are invalid", herr);
+    return A3D_OK;
+}
+
+int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, double *ms) {
+    const a3d_config &c = cfg;
+    if (s.sx < 0 || s.sx >= c.nx || s.sy < 0 || s.sy >= c.ny || s.sz < 0 || s.sz >= c.nz)
+        return fail(A3D_E_ARG, "shot (%d,%d,%d) outside the %dx%dx%d model", s.sx, s.sy, s.sz, c.nx, c.ny, c.nz);
+    if (!rec_dev) rec_dev = rec;
+    CUDA_TRY(cudaSetDevice(device));
+    CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    const size_t fb = g.elems() * esz;
+    // direct-wave mute thresholds for this shot
+    std::vector<int> mute;
+    if (c.mute) {
+        mute.resize((size_t)c.nx * c.ny);
+        for (int iy = 0; iy < c.ny; ++iy)
+            for (int ix = 0; ix < c.nx; ++ix)
+                mute[ix + (size_t)c.nx * iy] = mute_nt(ix, iy, s.sx, s.sy, s.sz, c.dx, c.dy, c.dz, c.dt, c.fm, v_mute);
+        CUDA_TRY(cudaMemcpyAsync(d_mute, mute.data(), mute.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+    auto snapshot = [&](int it, const void *field) -> int {
+        if (!hook || !hook->want || !hook->want(it)) return A3D_OK;
+        const int pad = g.pad;
+        if (fp64)
+            crop_window<double><<<1024, 256, 0, st>>>((const double *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx);
+        else
+            crop_window<float><<<1024, 256, 0, st>>>((const float *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx);
+        CUDA_TRY(cudaGetLastError());
+        snap_host.resize((size_t)c.nx * c.ny * c.nz);
+        CUDA_TRY(cudaMemcpyAsync(snap_host.data(), snap_dev, snap_host.size() * 4, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        return hook->take ? hook->take(it, snap_host.data()) : A3D_OK;
+    };
+    int rc;
+    if (c.physics == A3D_2ORDER) {
+        CUDA_TRY(cudaMemsetAsync(X, 0, fb, st));
+        CUDA_TRY(cudaMemsetAsync(Y, 0, fb, st));
+        const int pad = g.pad;
+        const int sxp = s.sx + pad, syp = s.sy + pad, szp = s.sz + pad;
+        // step 0's dipole into the zero current level (2O:443)
+        const size_t si = g.idx(szp, sxp, syp);
+        if (fp64) {
+            double d[3] = {(double)w2o[0], 0.0, -(double)w2o[0]};
+            CUDA_TRY(cudaMemcpyAsync((double *)X + si, d, sizeof d, cudaMemcpyHostToDevice, st));
+        } else {
+            float d[3] = {w2o[0], 0.0f, -w2o[0]};
+            CUDA_TRY(cudaMemcpyAsync((float *)X + si, d, sizeof d, cudaMemcpyHostToDevice, st));
+        }
+        K2OLaunch L{};
+        L.tx = tx;
+        L.fp64 = fp64;
+        L.grid = 0;
+        L.tm_vv = m2o_vv;
+        K2OParams &p = L.p;
+        p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
+        p.nx = c.nx; p.ny = c.ny;
+        p.gz = pad + c.rec_z; p.rx0 = pad; p.ry0 = pad;
+        p.fz = fz; p.fx = fx; p.fy = fy;
+        p.dz2 = (float)(1.0 / (double)(c.dz * c.dz));  // 2O:387-389
+        p.dx2 = (float)(1.0 / (double)(c.dx * c.dx));
+        p.dy2 = (float)(1.0 / (double)(c.dy * c.dy));
+        p.s_x = sxp; p.s_y = syp; p.s_z = szp;
+        p.rec = rec_dev;
+        p.mute_nt = c.mute ? d_mute : nullptr;
+        p.nt = c.nt;
+        p.err = d_err;
+        void *buf[2] = {X, Y};
+        int cur = 0;
+        CUDA_TRY(cudaEventRecord(ev0, st));
+        for (int it = 0; it < c.nt; ++it) {
+            L.tm_cur = m2o_cur[cur];
+            L.tm_prev = m2o_prev[1 - cur];
+            L.ybuf = buf[1 - cur];
+            p.w_next = it + 1 < c.nt ? w2o[it + 1] : 0.0f;
+            p.it = it;
+            CUDA_TRY(launch_k2o(L, st));
+            if ((rc = snapshot(it, buf[cur]))) return rc;
+            cur = 1 - cur;
+        }
+        CUDA_TRY(cudaEventRecord(ev1, st));
+    } else {
+        void *fields[11] = {u, v, w, P, Q, px, py, pz, qx, qy, qz};
+        for (void *f : fields)
+            if (f) CUDA_TRY(cudaMemsetAsync(f, 0, fb, st));
+        const int np = npml;
+        K1Launch Lv{}, Ls{};
+        K1Params p{};
+        p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
+        p.nx = c.nx; p.ny = c.ny; p.npml = np;
+        p.dtx = c.dt / c.dx; p.dty = c.dt / c.dy; p.dtz = c.dt / c.dz;
+        const float *q = pml;
+        p.cx1 = q; p.cx2 = q + g.nnx; p.ax1 = q + 2 * g.nnx; p.ax2 = q + 3 * g.nnx; q += 4 * g.nnx;
+        p.cy1 = q; p.cy2 = q + g.nny; p.ay1 = q + 2 * g.nny; p.ay2 = q + 3 * g.nny; q += 4 * g.nny;
+        p.cz1 = q; p.cz2 = q + g.nnz; p.az1 = q + 2 * g.nnz; p.az2 = q + 3 * g.nnz;
+        p.s_x = s.sx + np - 1; p.s_y = s.sy + np - 1; p.s_z = s.sz + np - 1;  // ..iso..:91-93
+        p.taper = taper;
+        p.px = px; p.py = py; p.pz = pz; p.qx = qx; p.qy = qy; p.qz = qz;
+        p.rec = rec_dev;
+        p.mute_nt = c.mute ? d_mute : nullptr;
+        p.nt = c.nt;
+        p.err = d_err;
+        const int kv = c.physics == A3D_ISO ? K1_ISO_VEL : (c.physics == A3D_VTI ? K1_VTI_VEL : K1_TTI_VEL);
+        Lv.kind = kv; Ls.kind = kv + 1;
+        Lv.maps = mvel; Lv.nmaps = nvel; Ls.maps = mstr; Ls.nmaps = nstr;
+        Lv.out0 = u; Lv.out1 = v; Lv.out2 = w;
+        Ls.out0 = P; Ls.out1 = Q;
+        Lv.tx = Ls.tx = tx; Lv.fp64 = Ls.fp64 = fp64; Lv.grid = Ls.grid = 0;
+        auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
+        CUDA_TRY(cudaEventRecord(ev0, st));
+        for (int it = 0; it < c.nt; ++it) {
+            p.it = it;
+            p.inj = inj[it];
+            p.amp0 = amp0[it];
+            p.amp1 = amp1[it];
+            Lv.p = p;
+            Ls.p = p;
+            CUDA_TRY(launch(Lv, st));
+            CUDA_TRY(launch(Ls, st));
+            if ((rc = snapshot(it, P))) return rc;
+        }
+        CUDA_TRY(cudaEventRecord(ev1, st));
+    }
+    if ((rc = check_kernel_error(this))) return rc;
+    if (ms) {
+        float f = 0;
+        CUDA_TRY(cudaEventElapsedTime(&f, ev0, ev1));
+        *ms = f;
+    }
+    return A3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C API
+
+static int validate(const a3d_config *c) {
+    if (!c) return fail(A3D_E_ARG, "null config");
+    if (c->physics < A3D_2ORDER || c->physics > A3D_TTI) return fail(A3D_E_ARG, "unknown physics %d", c->physics);
+    if (c->nx < 1 || c->ny < 1 || c->nz < 1 || c->nt < 1)
+        return fail(A3D_E_ARG, "grid %dx%dx%d, nt %d must be positive", c->nx, c->ny, c->nz, c->nt);
+    if (!(c->dx > 0) || !(c->dy > 0) || !(c->dz > 0) || !(c->dt > 0) || !(c->fm > 0))
+        return fail(A3D_E_ARG, "dx, dy, dz, dt and fm must be positive");
+    if (c->storage != A3D_FP32 && c->storage != A3D_FP64)
+        return fail(A3D_E_UNSUPPORTED, "storage type %d is not built for this engine", c->storage);
+    if (c->physics == A3D_ISO && (c->wtype < 1 || c->wtype > 6))
+        return fail(A3D_E_ARG, "wavelet type %d outside 1..6", c->wtype);
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const float *vel,
+                                 const float *rho, const float *eps, const float *del,
+                                 const float *theta, const float *phi, int device) {
+    clear_error();
+    if (!out) return fail(A3D_E_ARG, "null engine pointer");
+    *out = nullptr;
+    int rc = validate(cfg);
+    if (rc) return rc;
+    const int ph = cfg->physics;
+    if (!vel || (ph == A3D_ISO && !rho) || (ph == A3D_VTI && (!rho || !eps || !del)) ||
+        (ph == A3D_TTI && (!eps || !del || !theta || !phi)))
+        return fail(A3D_E_ARG, "a model array the physics reads is null");
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(A3D_E_ARG, "device %d not present (%d devices)", device, ndev);
+    CUDA_TRY(cudaSetDevice(device));
+    CUDA_TRY(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, device));
+    a3d_engine *e = new (std::nothrow) a3d_engine;
+    if (!e) return fail(A3D_E_NOMEM, "host allocation failed");
+    e->cfg = *cfg;
+    e->device = device;
+    e->fp64 = cfg->storage == A3D_FP64;
+    e->esz = e->fp64 ? 8 : 4;
+    e->tx = cfg->tile_x == 4 || cfg->tile_x == 16 ? cfg->tile_x : 8;
+    if (e->fp64 && e->tx == 16) e->tx = 8;
+    if (ph == A3D_2ORDER) {
+        e->npml = cfg->npml > 0 ? cfg->npml : 50;  // npd, 2O:19
+        if (e->cfg.rec_z < 0) e->cfg.rec_z = 1;    // 2O:159 records at model depth 1
+        if (e->cfg.rec_z >= cfg->nz) { delete e; return fail(A3D_E_ARG, "receiver depth %d outside the model", e->cfg.rec_z); }
+        e->g.set(cfg->nx, cfg->ny, cfg->nz, MM + e->npml);
+    } else {
+        e->npml = cfg->npml > 0 ? cfg->npml : (ph == A3D_TTI ? 40 : 20);
+        if (e->npml < 6) { delete e; return fail(A3D_E_ARG, "PML width %d below 6 cells", e->npml); }
+        e->g.set(cfg->nx, cfg->ny, cfg->nz, e->npml);
+    }
+    if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) {
+        delete e;
+        return fail(A3D_E_CUDA, "stream/event creation failed");
+    }
+    e->d_err = (int *)e->dalloc(sizeof(int) * 4);
+    if (!e->d_err) { delete e; return fail(A3D_E_NOMEM, "device allocation failed"); }
+    rc = engine_setup(e, vel, rho, eps, del, theta, phi);
+    if (rc) { delete e; return rc; }
+    *out = e;
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_destroy(a3d_engine *e) {
+    delete e;
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_run(a3d_engine *e, const a3d_shot *shot, float *rec_host, int snap_every,
+                              int snap_skip0, float *snaps_host, double *ms) {
+    clear_error();
+    if (!e || !shot) return fail(A3D_E_ARG, "null engine or shot");
+    if (snap_every < 0) return fail(A3D_E_ARG, "negative snapshot interval");
+    SnapHook hook;
+    int nsnap = 0;
+    const size_t win = (size_t)e->cfg.nx * e->cfg.ny * e->cfg.nz;
+    if (snap_every > 0 && snaps_host) {
+        hook.want = [&](int it) { return it % snap_every == 0 && !(snap_skip0 && it == 0); };
+        hook.take = [&](int, const float *d) {
+            memcpy(snaps_host + (size_t)nsnap * win, d, win * 4);
+            ++nsnap;
+            return A3D_OK;
+        };
+    }
+    int rc = e->run(*shot, nullptr, snap_every > 0 && snaps_host ? &hook : nullptr, ms);
+    if (rc) return rc;
+    if (rec_host) {
+        cudaError_t ce = cudaMemcpy(rec_host, e->rec, (size_t)e->cfg.nt * e->cfg.nx * e->cfg.ny * 4, cudaMemcpyDeviceToHost);
+        if (ce != cudaSuccess) return fail(A3D_E_CUDA, "record copy failed: %s", cudaGetErrorString(ce));
+    }
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_run_device(a3d_engine *e, const a3d_shot *shot, float *rec_dev, double *ms) {
+    clear_error();
+    if (!e || !shot) return fail(A3D_E_ARG, "null engine or shot");
+    return e->run(*shot, rec_dev, nullptr, ms);
+}
+
+extern "C" float *a3d_engine_record_device(a3d_engine *e) { return e ? e->rec : nullptr; }
+
+extern "C" size_t a3d_engine_device_bytes(const a3d_engine *e) { return e ? e->dev_bytes : 0; }
+
+extern "C" int a3d_forward_host(const a3d_config *cfg, const float *vel, const float *rho, const float *eps,
+                                const float *del, const float *theta, const float *phi,
+                                const a3d_shot *shots, int nshot, float *recs_host, int device) {
+    a3d_engine *e = nullptr;
+    int rc = a3d_engine_create(&e, cfg, vel, rho, eps, del, theta, phi, device);
+    if (rc) return rc;
+    const size_t nrec = (size_t)cfg->nt * cfg->nx * cfg->ny;
+    for (int i = 0; i < nshot && !rc; ++i)
+        rc = a3d_engine_run(e, &shots[i], recs_host ? recs_host + i * nrec : nullptr, 0, 0, nullptr, nullptr);
+    a3d_engine_destroy(e);
+    return rc;
+}
+
+extern "C" const char *a3d_last_error(void) { return a3d::g_err.c_str(); }

@@ -1,0 +1,71 @@
+// a3d_engine.h — the engine object behind the C ABI.
+#pragma once
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "../../include/acoustic3d.h"
+#include "a3d_k1.cuh"
+#include "a3d_setup.h"
+
+namespace a3d {
+
+// thread-local last-error text; fail() records it, prints it and returns code
+int fail(int code, const char *fmt, ...);
+void clear_error();
+
+// snapshot hook: want(it) says whether a snapshot is taken after step it;
+// take(it, window) receives the model window (nz*nx*ny floats, z fastest)
+struct SnapHook {
+    std::function<bool(int)> want;
+    std::function<int(int, const float *)> take;
+};
+
+}  // namespace a3d
+
+struct a3d_engine {
+    a3d_config cfg{};
+    a3d::Grid g;
+    int device = 0;
+    int npml = 0;          // absorber cells (1st order) or sponge width npd (2nd order)
+    int tx = 8;
+    bool fp64 = false;
+    size_t esz = 4;        // bytes per wavefield element
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int *d_err = nullptr;
+    std::vector<void *> allocs;
+    size_t dev_bytes = 0;
+
+    // model parameters on the device (float, padded layout)
+    float *vv = nullptr, *vp = nullptr, *rho = nullptr, *eps = nullptr, *del = nullptr;
+    float *tct = nullptr, *tst = nullptr, *tcp = nullptr, *tsp = nullptr;  // TTI trig
+    float v_mute = 0.0f;   // direct-wave mute velocity
+
+    // wavefields
+    void *X = nullptr, *Y = nullptr;                          // 2nd order
+    void *u = nullptr, *v = nullptr, *w = nullptr, *P = nullptr, *Q = nullptr;
+    void *px = nullptr, *py = nullptr, *pz = nullptr, *qx = nullptr, *qy = nullptr, *qz = nullptr;
+
+    // coefficients
+    float2 *fz = nullptr, *fx = nullptr, *fy = nullptr;       // 2nd-order sponge
+    float *pml = nullptr;  // cx1 cx2 ax1 ax2 | cy1 cy2 ay1 ay2 | cz1 cz2 az1 az2 blocks
+    float2 *taper = nullptr;
+    std::vector<float> w2o;                    // 2nd-order Ricker samples
+    std::vector<float> amp0, amp1;             // 1st-order injected amplitudes per step
+    std::vector<int> inj;                      // 1st-order: inject at step it
+
+    float *rec = nullptr;   // [ny][nx][nt]
+    int *d_mute = nullptr;  // first unmuted sample per trace
+    float *snap_dev = nullptr;
+    std::vector<float> snap_host;
+
+    // tensor maps
+    CUtensorMap m2o_cur[2], m2o_prev[2], m2o_vv;
+    CUtensorMap mvel[9], mstr[12];
+    int nvel = 0, nstr = 0;
+
+    ~a3d_engine();
+    void *dalloc(size_t bytes);  // zeroed; null on failure
+    int run(const a3d_shot &s, float *rec_dev, const a3d::SnapHook *hook, double *ms);
+};

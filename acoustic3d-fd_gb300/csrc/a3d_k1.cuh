@@ -1,0 +1,52 @@
+// a3d_k1.cuh — parameter block and launch entry points of the 1st-order
+// (staggered-grid) engines: isotropic, VTI and TTI.
+#pragma once
+#include "a3d_kernels.cuh"
+
+namespace a3d {
+
+struct K1Params {
+    Sweep sw;
+    int nnz, nnx, nny, ldz;
+    int nx, ny, npml;
+    float dtx, dty, dtz;                              // dt/dx, dt/dy, dt/dz (float, as the reference)
+    const float *cx1, *cx2, *cy1, *cy2, *cz1, *cz2;   // velocity PML coefficients (half cell)
+    const float *ax1, *ax2, *ay1, *ay2, *az1, *az2;   // pressure PML coefficients (integer cell)
+    // source cell in padded coordinates; the isotropic dipole's second pole is s_z + 2
+    int s_x, s_y, s_z;
+    int inj;                 // inject this step (t <= 2/fm)
+    float amp0, amp1;        // isotropic: added at s_z and at s_z+2; VTI/TTI: added to P and Q
+    const float2 *taper;     // SV ball: hi/lo of the epsilon/delta factor for r^2 = 0..225
+    // split (PML) components, touched only on damped axes
+    void *px, *py, *pz, *qx, *qy, *qz;
+    // record at model depth 0 (padded z = npml)
+    float *rec;
+    const int *mute_nt;
+    int it, nt;
+    int *err;
+};
+
+enum K1Kind { K1_ISO_VEL = 0, K1_ISO_STR, K1_VTI_VEL, K1_VTI_STR, K1_TTI_VEL, K1_TTI_STR };
+
+// tensor-map box shapes: core {32,TX}, x-halo {32,TX+8}, z-halo {40,TX}, both {40,TX+8}
+enum Box { BOX_CORE = 0, BOX_HX = 1, BOX_HZ = 2, BOX_H = 3 };
+
+struct K1Launch {
+    int kind;
+    const CUtensorMap *maps;  // in the order the kernel documents
+    int nmaps;
+    void *out0, *out1, *out2;  // fields written (vel: u,v,w; stress: P[,Q])
+    K1Params p;
+    int tx, grid;
+    bool fp64;
+};
+
+cudaError_t launch_k1(const K1Launch &L, cudaStream_t st);
+
+}  // namespace a3d
+
+namespace a3d {
+cudaError_t launch_iso(const K1Launch &L, cudaStream_t st);
+cudaError_t launch_vti(const K1Launch &L, cudaStream_t st);
+cudaError_t launch_tti(const K1Launch &L, cudaStream_t st);
+}  // namespace a3d

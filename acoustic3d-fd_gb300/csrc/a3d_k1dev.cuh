@@ -1,0 +1,71 @@
+// a3d_k1dev.cuh — device helpers shared by the 1st-order kernels.
+#pragma once
+#include "a3d_k1.cuh"
+#include "a3d_pipe.cuh"
+
+namespace a3d {
+
+template <int N> struct Maps { CUtensorMap m[N]; };
+
+template <class S>
+__device__ __forceinline__ size_t gidx(const K1Params &p, int iz, int ix, int iy) {
+    return (size_t)iz + (size_t)p.ldz * ((size_t)ix + (size_t)p.nnx * iy);
+}
+
+// the damped-axis pressure update shared by every 1st-order engine; the oracle's
+// engine form (a3d_oracle_loops.inc, engine_pupdate) performs the same operations
+template <class T, class S>
+__device__ __forceinline__ T pupdate(T Pold, T gx, T gy, T gz, bool dx, bool dy, bool dz,
+                                     float ax2, float ay2, float az2, S *cx, S *cy, S *cz,
+                                     size_t g) {
+    if (!(dx | dy | dz)) return ((Pold - gx) - gy) - gz;
+    T vx = dx ? from_store<T, S>(cx[g]) : T(0);
+    T vy = dy ? from_store<T, S>(cy[g]) : T(0);
+    T vz = dz ? from_store<T, S>(cz[g]) : T(0);
+    T s = Pold;
+    if (dx) s = s - vx;
+    if (dy) s = s - vy;
+    if (dz) s = s - vz;
+    if (!dx) s = s - gx;
+    if (!dy) s = s - gy;
+    if (!dz) s = s - gz;
+    if (dx) { vx = fma_t((T)ax2, vx, -gx); s = s + vx; cx[g] = to_store<S, T>(vx); }
+    if (dy) { vy = fma_t((T)ay2, vy, -gy); s = s + vy; cy[g] = to_store<S, T>(vy); }
+    if (dz) { vz = fma_t((T)az2, vz, -gz); s = s + vz; cz[g] = to_store<S, T>(vz); }
+    return s;
+}
+
+__device__ __forceinline__ bool damped(float a1, float a2) { return !(a1 == 1.0f && a2 == 1.0f); }
+
+
+// launch helper: sets the smem attribute once, sizes the grid, launches
+template <class Kern, class... Args>
+static cudaError_t k1_launch(Kern kern, int nthreads, size_t smem, long long W, int grid,
+                             cudaStream_t st, bool &attr_done, Args... args) {
+    if (!attr_done) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_done = true;
+    }
+    if (grid <= 0) {
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nthreads, smem);
+        grid = occ_grid(occ, W);
+    }
+    kern<<<grid, nthreads, smem, st>>>(args...);
+    return cudaGetLastError();
+}
+
+template <int TX>
+static void k1_sweep(K1Params &p) {
+    p.sw.ntz = (p.nnz - 2 * MM + 31) / 32;
+    p.sw.ntx = (p.nnx - 2 * MM + TX - 1) / TX;
+    p.sw.y_begin = MM;
+    p.sw.NY = p.nny - 2 * MM;
+    p.sw.W = (long long)p.sw.ntz * p.sw.ntx * p.sw.NY;
+}
+
+// loads of a stored field value / smem tile element as the arithmetic type
+template <class T, class S> __device__ __forceinline__ T ld(const S *a, int i) { return from_store<T, S>(a[i]); }
+
+}  // namespace a3d

@@ -1,0 +1,68 @@
+// a3d_kernels.cuh — parameter blocks and launch entry points of the stencil
+// kernels, shared between the kernel translation units and the host engine.
+#pragma once
+#include <cudaTypedefs.h>
+
+#include "a3d_common.cuh"
+
+namespace a3d {
+
+// 8th-order second-derivative coefficients (Toa_3dfd_cuda.cu:32), float-rounded
+constexpr float S8_0 = (float)(-205.0 / 72.0), S8_1 = (float)(8.0 / 5.0),
+                S8_2 = (float)(-1.0 / 5.0), S8_3 = (float)(8.0 / 315.0),
+                S8_4 = (float)(-1.0 / 560.0);
+// 8th-order staggered first-derivative coefficients (..iso..:37), float-rounded
+constexpr float C8_0 = 1.196289f, C8_1 = -0.0797526f, C8_2 = 0.009570313f,
+                C8_3 = -0.0006975447f;
+
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// sponge multiply on the y, x, z faces in that order (Toa_3dfd_cuda.cu:138-151);
+// a face factor is stored as hi+lo floats of the double factor, hi == 0: no face
+template <class T> __device__ __forceinline__ T sponge1(T v, float2 f);
+template <> __device__ __forceinline__ float sponge1<float>(float v, float2 f) {
+    return f.x != 0.0f ? mul_df(v, f.x, f.y) : v;
+}
+template <> __device__ __forceinline__ double sponge1<double>(double v, float2 f) {
+    return f.x != 0.0f ? ((double)f.x + (double)f.y) * v : v;
+}
+template <class T>
+__device__ __forceinline__ T sponge3(T v, float2 fy, float2 fx, float2 fz) {
+    return sponge1<T>(sponge1<T>(sponge1<T>(v, fy), fx), fz);
+}
+
+// ---------------------------------------------------------------------------
+// 2nd-order step
+struct K2OParams {
+    Sweep sw;
+    int nnz, nnx, nny, ldz;
+    int nx, ny;           // model (receiver grid) size
+    int gz, rx0, ry0;     // receiver depth and first receiver column/row (padded coords)
+    const float2 *fz, *fx, *fy;  // sponge factors per axis
+    float dz2, dx2, dy2;  // 1/d^2
+    int s_x, s_y, s_z;    // dipole cell (padded coords); the second pole is s_z + 2
+    float w_next;         // dipole amplitude of the next step (0 after the last)
+    float *rec;           // record [ny][nx][nt]
+    const int *mute_nt;   // first unmuted sample per trace, or null
+    int it, nt;
+    int *err;
+};
+
+struct K2OLaunch {
+    CUtensorMap tm_cur, tm_prev, tm_vv;
+    void *ybuf;  // previous-level buffer, overwritten with the next level
+    K2OParams p;
+    int tx;      // tile width along x (4, 8, 16)
+    int grid;    // CTAs (0: one wave at full occupancy)
+    bool fp64;
+};
+
+cudaError_t launch_k2o(const K2OLaunch &L, cudaStream_t st);
+size_t k2o_smem_bytes(int tx, bool fp64);
+
+// CTAs for a sweep of W plane-units: one full wave at the given occupancy, but
+// at least ~24 output planes per CTA so the 8-plane warm-up stays cheap
+int occ_grid(int occ_per_sm, long long W);
+
+}  // namespace a3d

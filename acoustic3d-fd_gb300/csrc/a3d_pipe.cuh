@@ -1,0 +1,136 @@
+// a3d_pipe.cuh — the y-marching TMA pipeline shared by every stencil kernel.
+//
+// A CTA owns a contiguous range of the sweep's (tile, plane) space (cta_range),
+// split into segments of consecutive output planes [ya, yb) of one 32 x TX tile.
+// For each segment it streams planes q = ya-4 .. yb+3 ("A items": the fields
+// whose y-derivative is taken, kept in a 9-plane register window) and, for
+// q >= ya+4, the output plane o = q-4 ("B items": everything else the update at
+// plane o reads).  One producer thread issues the TMA copies into two mbarrier
+// rings; the consumer warps (one 32-cell z row each) wait, compute, release.
+//
+//   A stage of item j is read at its own arrival (window push) and 4 items later
+//   (in-plane neighbours of output plane q-4), then released: KA >= 5.
+//   B stage is released right after the output plane is computed.
+//
+// Every wait is bounded (mbar_wait); a timeout records an error code, raises a
+// CTA-wide abort flag so the other role stops, and the producer drains all
+// copies it issued before the CTA exits.
+#pragma once
+#include "a3d_common.cuh"
+
+namespace a3d {
+
+template <int KA, int KB>
+struct PipeBars {
+    uint64_t fullA[KA], emptyA[KA], fullB[KB], emptyB[KB];
+    int abort_flag;
+    __device__ void init(int nconsumers) {
+        for (int i = 0; i < KA; ++i) { mbar_init(&fullA[i], 1); mbar_init(&emptyA[i], nconsumers); }
+        for (int i = 0; i < KB; ++i) { mbar_init(&fullB[i], 1); mbar_init(&emptyB[i], nconsumers); }
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    __device__ volatile int *abort_ptr() { return &abort_flag; }
+};
+
+struct Seg {
+    int tile, ya, yb, z0, x0;
+};
+
+template <int TX>
+__device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long w1, long long &wend) {
+    Seg s;
+    s.tile = (int)(w / sw.NY);
+    s.ya = sw.y_begin + (int)(w % sw.NY);
+    wend = (long long)(s.tile + 1) * sw.NY;
+    if (wend > w1) wend = w1;
+    s.yb = s.ya + (int)(wend - w);
+    s.z0 = MM + 32 * (s.tile % sw.ntz);
+    s.x0 = MM + TX * (s.tile / sw.ntz);
+    return s;
+}
+
+// Producer: one thread.  issueA(stage_ptr, bar, seg, q) / issueB(stage_ptr, bar, seg, o)
+// issue the copies of one item (the expect_tx byte counts are bytesA / bytesB).
+template <int TX, int KA, int KB, class IssueA, class IssueB>
+__device__ __forceinline__ void pipe_produce(const Sweep &sw, long long w0, long long w1,
+                                             PipeBars<KA, KB> &b, unsigned char *ringA,
+                                             size_t strideA, uint32_t bytesA, unsigned char *ringB,
+                                             size_t strideB, uint32_t bytesB, int *err,
+                                             IssueA issueA, IssueB issueB) {
+    volatile int *ab = b.abort_ptr();
+    long long ja = 0, jb = 0;
+    bool ok = true;
+    for (long long w = w0; w < w1 && ok;) {
+        long long wend;
+        const Seg s = make_seg<TX>(sw, w, w1, wend);
+        for (int q = s.ya - MM; q < s.yb + MM; ++q) {
+            const int sa = (int)(ja % KA);
+            if (ja >= KA)
+                ok = mbar_wait(&b.emptyA[sa], (uint32_t)(((ja / KA) - 1) & 1), err,
+                               KERR_EMPTY_TIMEOUT, ab);
+            if (!ok) break;
+            mbar_arrive_expect_tx(&b.fullA[sa], bytesA);
+            issueA(ringA + sa * strideA, &b.fullA[sa], s, q);
+            ++ja;
+            const int o = q - MM;
+            if (o >= s.ya) {
+                const int sb = (int)(jb % KB);
+                if (jb >= KB)
+                    ok = mbar_wait(&b.emptyB[sb], (uint32_t)(((jb / KB) - 1) & 1), err,
+                                   KERR_EMPTY_TIMEOUT, ab);
+                if (!ok) break;
+                mbar_arrive_expect_tx(&b.fullB[sb], bytesB);
+                issueB(ringB + sb * strideB, &b.fullB[sb], s, o);
+                ++jb;
+            }
+        }
+        w = wend;
+    }
+    // drain: every issued copy must land before the CTA's shared memory goes away
+    for (long long j = (ja > KA ? ja - KA : 0); j < ja; ++j)
+        if (!mbar_wait(&b.fullA[j % KA], (uint32_t)((j / KA) & 1), err, KERR_DRAIN_TIMEOUT, ab))
+            break;
+    for (long long j = (jb > KB ? jb - KB : 0); j < jb; ++j)
+        if (!mbar_wait(&b.fullB[j % KB], (uint32_t)((j / KB) & 1), err, KERR_DRAIN_TIMEOUT, ab))
+            break;
+}
+
+// Consumers: all consumer threads.  onSeg(seg) at a segment start; onLoad(stageA, seg, q)
+// when A item q arrived; onOut(stageA_of_o, stageB, seg, o) for each output plane.
+// Returns false on abort.
+template <int TX, int KA, int KB, class OnSeg, class OnLoad, class OnOut>
+__device__ __forceinline__ bool pipe_consume(const Sweep &sw, long long w0, long long w1,
+                                             PipeBars<KA, KB> &b, unsigned char *ringA,
+                                             size_t strideA, unsigned char *ringB, size_t strideB,
+                                             int *err, OnSeg onSeg, OnLoad onLoad, OnOut onOut) {
+    volatile int *ab = b.abort_ptr();
+    long long ja = 0, jb = 0;
+    for (long long w = w0; w < w1;) {
+        long long wend;
+        const Seg s = make_seg<TX>(sw, w, w1, wend);
+        onSeg(s);
+        for (int q = s.ya - MM; q < s.yb + MM; ++q) {
+            const int sa = (int)(ja % KA);
+            if (!mbar_wait(&b.fullA[sa], (uint32_t)((ja / KA) & 1), err, KERR_FULL_TIMEOUT, ab))
+                return false;
+            onLoad(ringA + sa * strideA, s, q);
+            const int o = q - MM;
+            if (o >= s.ya) {
+                const int sb = (int)(jb % KB);
+                if (!mbar_wait(&b.fullB[sb], (uint32_t)((jb / KB) & 1), err, KERR_FULL_TIMEOUT,
+                               ab))
+                    return false;
+                onOut(ringA + ((ja - MM) % KA) * strideA, ringB + sb * strideB, s, o);
+                mbar_arrive(&b.emptyB[sb]);
+                ++jb;
+            }
+            if (ja >= MM) mbar_arrive(&b.emptyA[(ja - MM) % KA]);
+            ++ja;
+        }
+        w = wend;
+    }
+    return true;
+}
+
+}  // namespace a3d

@@ -1,0 +1,151 @@
+/*
+ * acoustic3d.h — C ABI of the GB300 (sm_103a) acoustic finite-difference engines.
+ *
+ * Two layers:
+ *
+ * 1. Drop-in entry points with the names and argument lists of the reference's
+ *    four shared libraries (paths relative to the reference project).  The build
+ *    produces lib/acoustic2order.so, lib/acoustic1order.so, lib/acoustic1vti.so and
+ *    lib/acoustic1tti.so; each exports all four symbols, so readmodel.py's
+ *    cdll.LoadLibrary('./lib/<name>.so') + <symbol>(...) calls work unchanged.
+ *    They read the same raw float32 model files and write byte-identical shot
+ *    records and snapshots.  Unlike the reference they never exit() the process:
+ *    they return an int status (0 ok, A3D_E_* otherwise, message on stderr); a
+ *    ctypes caller that sets no restype ignores it, as it ignored the void.
+ *
+ * 2. An in-memory engine API (a3d_*) used by the tests and benchmarks: the model
+ *    is uploaded once into device memory and any number of shots run against it.
+ *
+ * Model arrays are float32, nx*ny*nz, z fastest, then x, then y (the reference's
+ * file order, readmodel.py / ..iso..:249-257).  Records are float32
+ * [ny][nx][nt], time fastest (the reference's internal record layout).
+ */
+#ifndef ACOUSTIC3D_H
+#define ACOUSTIC3D_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- statuses */
+#define A3D_OK 0
+#define A3D_E_ARG 1         /* invalid argument or geometry                         */
+#define A3D_E_IO 2          /* model, record or snapshot file could not be opened/read/written */
+#define A3D_E_CUDA 3        /* CUDA runtime error (message names the call)          */
+#define A3D_E_NOMEM 4       /* host or device allocation failed                     */
+#define A3D_E_KERNEL 5      /* a kernel gave up a bounded wait (error word set)     */
+#define A3D_E_UNSUPPORTED 6 /* combination not built (e.g. storage type for physics) */
+
+/* ------------------------------------------------- drop-in entry points */
+
+/* Replaces cuda_3dfd, src/Toa_3dfd_cuda.cu:366-370 (lib/acoustic2order.so).
+ * 2nd-order 8th-order-Laplacian leap-frog, 50-cell sponge, z-dipole source,
+ * receivers on every surface node at model depth 1.  As in the reference,
+ * kt, snap_interval and cut_directwave are ignored (readmodel.py passes the last
+ * two in swapped positions, readmodel.py:335-338) and snapshots, when
+ * show_snapshot is set, are taken every 500 steps as FNsnap"ishot_<is>_it_<it>.bin". */
+int cuda_3dfd(char *FNvel, char *FNsnap, char *FNshot, int is, int ns, int nx, int ny, int nz,
+              float dx, float dy, float dz, int sxbeg, int sybeg, int szbeg, int jsx, int jsy,
+              int jsz, float dgx, float dgy, float dgt, int nt, int kt, float dt, float fm,
+              bool show_snapshot, bool cut_directwave, int snap_interval, int cudaDevicei);
+
+/* Replaces cuda_3dfd_1order, src/Toa_gpu_3diso_fd_1orderfunciton.cu:372-377
+ * (lib/acoustic1order.so).  Staggered-grid pressure/particle-velocity with
+ * density, 20-cell split PML, dipole source (wavelet wtype 1..6), receivers at
+ * model depth 0, optional direct-wave mute; ns shots along x (is = 0..ns-1), each
+ * record written at byte offset is*nt*nx*ny*4.  Snapshots every snap_interval
+ * steps as FNsnap"ishot_<is>it_<it>.bin" (no underscore, as the reference). */
+int cuda_3dfd_1order(char *FNvel, char *FNrho, char *FNsnap, char *FNshot, int is, int ns,
+                     int nx, int ny, int nz, float dx, float dy, float dz, int sxbeg, int sybeg,
+                     int szbeg, int jsx, int jsy, int jsz, float dgx, float dgy, float dgt, int nt,
+                     float dt, int wtype, float fm, bool show_snapshot, bool cut_directwave,
+                     int snap_interval, int cudaDevicei);
+
+/* Replaces cuda_3dfd_vti, src/Toa_gpu_3dvti_fd_1orderfunciton.cu:389-395
+ * (lib/acoustic1vti.so).  Pseudo-acoustic VTI (P, Q) with density, epsilon,
+ * delta, SV-suppression ball round the source, 20-cell PML, Ricker monopole into
+ * P and Q.  Snapshots as FNsnap"ishot_<is>_it_<it>.bin". */
+int cuda_3dfd_vti(char *FNvel, char *FNrho, char *FNepsilon, char *FNdelta, char *FNsnap,
+                  char *FNshot, int is, int ns, int nx, int ny, int nz, float dx, float dy,
+                  float dz, int sxbeg, int sybeg, int szbeg, int jsx, int jsy, int jsz, float dgx,
+                  float dgy, float dgt, int nt, float dt, float fm, bool show_snapshot,
+                  bool cut_directwave, int snap_interval, int cudaDevicei);
+
+/* Replaces cuda_3dfd_tti, src/Toa_gpu_3dtti_fd_1orderfunciton.cu:390-398
+ * (lib/acoustic1tti.so).  Pseudo-acoustic TTI with tilt theta and azimuth psi
+ * (radians), no density (FNrho is ignored), 40-cell PML, ns forced to 1;
+ * snapshots every 100 steps for it != 0 whatever show_snapshot says.
+ * Returns 1 when the shot file cannot be opened, as the reference does. */
+int cuda_3dfd_tti(char *FNvel, char *FNrho, char *FNepsilon, char *FNdelta, char *FNtheta,
+                  char *FNpsi, char *FNsnap, char *FNshot, int is, int ns, int nx, int ny, int nz,
+                  float dx, float dy, float dz, int sxbeg, int sybeg, int szbeg, int jsx, int jsy,
+                  int jsz, float dgx, float dgy, float dgt, int nt, float dt, float fm,
+                  bool show_snapshot, bool cut_directwave, int snap_interval, int cudaDevicei);
+
+/* ------------------------------------------------------- engine API */
+
+enum a3d_physics { A3D_2ORDER = 0, A3D_ISO = 1, A3D_VTI = 2, A3D_TTI = 3 };
+enum a3d_storage { A3D_FP32 = 0, A3D_BF16 = 1, A3D_FP16 = 2, A3D_FP64 = 3 };
+
+typedef struct {
+    int physics;       /* enum a3d_physics                                        */
+    int nx, ny, nz;    /* model grid                                              */
+    float dx, dy, dz;  /* spacing (m)                                             */
+    int nt;            /* time steps                                              */
+    float dt, fm;      /* step (s), Ricker peak frequency (Hz)                    */
+    int wtype;         /* isotropic source wavelet 1..6 (others use 1)            */
+    int npml;          /* absorber cells; <= 0 selects the reference's value:
+                          50 (2nd-order sponge), 20 (iso, VTI), 40 (TTI)          */
+    int rec_z;         /* 2nd order: receiver depth in model cells; < 0: 1        */
+    int mute;          /* zero the direct wave in the record                      */
+    int storage;       /* enum a3d_storage of the wavefields (FP32 or FP64 here)  */
+    int tile_x;        /* kernel tile width along x (4, 8, 16); 0: default        */
+} a3d_config;
+
+typedef struct {
+    int sx, sy, sz;    /* shot position in model cells (sxbeg, sybeg, szbeg)      */
+} a3d_shot;
+
+typedef struct a3d_engine a3d_engine;
+
+/* Create an engine on `device` and upload the model.  Arrays the physics does
+ * not read may be NULL (2nd order: vel; iso: vel, rho; VTI: vel, rho, eps, del;
+ * TTI: vel, eps, del, theta, phi). */
+int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const float *vel,
+                      const float *rho, const float *eps, const float *del, const float *theta,
+                      const float *phi, int device);
+int a3d_engine_destroy(a3d_engine *e);
+
+/* Run one shot.  rec_host: nt*nx*ny floats (or NULL).  If snap_every > 0, a
+ * snapshot (model window, nz*nx*ny floats, z fastest) is copied into snaps_host
+ * after every step with it % snap_every == 0 (it != 0 too when snap_skip0).
+ * *ms (optional) receives the device time of the time loop (CUDA events). */
+int a3d_engine_run(a3d_engine *e, const a3d_shot *shot, float *rec_host, int snap_every,
+                   int snap_skip0, float *snaps_host, double *ms);
+
+/* Run one shot leaving the record on the device: rec_dev is a device pointer to
+ * nt*nx*ny floats (or NULL to keep the engine's own buffer); no host copies. */
+int a3d_engine_run_device(a3d_engine *e, const a3d_shot *shot, float *rec_dev, double *ms);
+
+/* Device pointer of the engine's record buffer ([ny][nx][nt] floats). */
+float *a3d_engine_record_device(a3d_engine *e);
+
+/* Bytes the engine holds in device memory. */
+size_t a3d_engine_device_bytes(const a3d_engine *e);
+
+/* Everything in one call from host buffers: create, run the shots, copy their
+ * records into recs_host (nshot * nt*nx*ny floats), destroy. */
+int a3d_forward_host(const a3d_config *cfg, const float *vel, const float *rho, const float *eps,
+                     const float *del, const float *theta, const float *phi,
+                     const a3d_shot *shots, int nshot, float *recs_host, int device);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char *a3d_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

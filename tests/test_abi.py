@@ -1,0 +1,50 @@
+"""CPU checks of the C ABI: the libraries build, load, and export every symbol
+include/acoustic3d.h declares; argument validation runs before any GPU work."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import PKG, ROOT
+
+HEADER = os.path.join(ROOT, "include", "acoustic3d.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?(?:int|float\s*\*|size_t|char\s*\*|void)\s+\**(\w+)\s*\(",
+                                 src, flags=re.M)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for need in ("cuda_3dfd", "cuda_3dfd_1order", "cuda_3dfd_vti", "cuda_3dfd_tti",
+                 "a3d_engine_create", "a3d_engine_run", "a3d_engine_destroy", "a3d_forward_host"):
+        assert need in names
+
+
+@pytest.mark.parametrize("libname", ["libacoustic3d.so", "acoustic2order.so", "acoustic1order.so",
+                                     "acoustic1vti.so", "acoustic1tti.so"])
+def test_library_exports_every_declared_symbol(engine_lib, libname):
+    lib = ctypes.CDLL(os.path.join(PKG, "lib", libname))
+    for name in declared_functions():
+        assert hasattr(lib, name), f"{libname} does not export {name}"
+
+
+def test_invalid_config_rejected_without_gpu(engine_lib):
+    import a3d
+    cfg = a3d.make_config("iso", 0, 10, 10)  # nx = 0
+    h = ctypes.c_void_p()
+    rc = a3d.lib().a3d_engine_create(ctypes.byref(h), ctypes.byref(cfg), *[a3d._fptr(None)] * 6, 0)
+    assert rc == a3d.A3D_E_ARG
+    assert "must be positive" in a3d.last_error()
+
+
+def test_unsupported_storage_rejected(engine_lib):
+    import a3d
+    cfg = a3d.make_config("iso", 10, 10, 10, storage=7)
+    h = ctypes.c_void_p()
+    rc = a3d.lib().a3d_engine_create(ctypes.byref(h), ctypes.byref(cfg), *[a3d._fptr(None)] * 6, 0)
+    assert rc == a3d.A3D_E_UNSUPPORTED
