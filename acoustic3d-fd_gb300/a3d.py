@@ -73,6 +73,10 @@ def lib() -> ctypes.CDLL:
         L.a3d_forward_host.argtypes = [ctypes.POINTER(Config)] + [_FP] * 6 + [ctypes.POINTER(ShotPos),
                                                                                ctypes.c_int, _FP, ctypes.c_int]
         L.a3d_forward_host.restype = ctypes.c_int
+        L.a3d_engine_set_profiling.argtypes = [vp, ctypes.c_int]
+        L.a3d_engine_set_profiling.restype = ctypes.c_int
+        L.a3d_engine_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]
+        L.a3d_engine_kernel_times.restype = ctypes.c_int
         L.a3d_last_error.argtypes = []
         L.a3d_last_error.restype = ctypes.c_char_p
         _lib = L
@@ -158,6 +162,16 @@ class Engine:
         _check(lib().a3d_engine_run_device(self.h, ctypes.byref(ShotPos(sx, sy, sz)),
                                            ctypes.c_void_p(rec_dev_ptr), ctypes.byref(ms)))
         return ms.value
+
+    def set_profiling(self, on: bool):
+        _check(lib().a3d_engine_set_profiling(self.h, int(on)))
+
+    def kernel_times(self):
+        """([ms_vel_or_step, ms_stress], [launches, launches]) summed since profiling was enabled."""
+        ms = (ctypes.c_double * 2)()
+        n = (ctypes.c_longlong * 2)()
+        _check(lib().a3d_engine_kernel_times(self.h, ms, n))
+        return [ms[0], ms[1]], [n[0], n[1]]
 
     def record_device_ptr(self) -> int:
         return lib().a3d_engine_record_device(self.h)

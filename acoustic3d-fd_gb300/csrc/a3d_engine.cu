@@ -99,6 +99,7 @@ using namespace a3d;
 
 a3d_engine::~a3d_engine() {
     if (st) cudaStreamSynchronize(st);
+    for (cudaEvent_t ev : kev) cudaEventDestroy(ev);
     for (void *p : allocs) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -300,6 +301,17 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     return A3D_OK;
 }
 
+static int prepare_profiling(a3d_engine *e, int per_step) {
+    if (!e->profiling) return A3D_OK;
+    const size_t need = (size_t)per_step * e->cfg.nt;
+    while (e->kev.size() < need) {
+        cudaEvent_t ev;
+        CUDA_TRY(cudaEventCreate(&ev));
+        e->kev.push_back(ev);
+    }
+    return A3D_OK;
+}
+
 static int check_kernel_error(a3d_engine *e) {
     int herr = 0;
     CUDA_TRY(cudaMemcpyAsync(&herr, e->d_err, sizeof(int), cudaMemcpyDeviceToHost, e->st));
@@ -374,6 +386,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         p.err = d_err;
         void *buf[2] = {X, Y};
         int cur = 0;
+        if ((rc = prepare_profiling(this, 2))) return rc;
         CUDA_TRY(cudaEventRecord(ev0, st));
         for (int it = 0; it < c.nt; ++it) {
             L.tm_cur = m2o_cur[cur];
@@ -381,7 +394,9 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
             L.ybuf = buf[1 - cur];
             p.w_next = it + 1 < c.nt ? w2o[it + 1] : 0.0f;
             p.it = it;
+            if (profiling) CUDA_TRY(cudaEventRecord(kev[2 * it], st));
             CUDA_TRY(launch_k2o(L, st));
+            if (profiling) CUDA_TRY(cudaEventRecord(kev[2 * it + 1], st));
             if ((rc = snapshot(it, buf[cur]))) return rc;
             cur = 1 - cur;
         }
@@ -414,6 +429,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         Ls.out0 = P; Ls.out1 = Q;
         Lv.tx = Ls.tx = tx; Lv.fp64 = Ls.fp64 = fp64; Lv.grid = Ls.grid = 0;
         auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
+        if ((rc = prepare_profiling(this, 3))) return rc;
         CUDA_TRY(cudaEventRecord(ev0, st));
         for (int it = 0; it < c.nt; ++it) {
             p.it = it;
@@ -422,13 +438,26 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
             p.amp1 = amp1[it];
             Lv.p = p;
             Ls.p = p;
+            if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it], st));
             CUDA_TRY(launch(Lv, st));
+            if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 1], st));
             CUDA_TRY(launch(Ls, st));
+            if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 2], st));
             if ((rc = snapshot(it, P))) return rc;
         }
         CUDA_TRY(cudaEventRecord(ev1, st));
     }
     if ((rc = check_kernel_error(this))) return rc;
+    if (profiling) {
+        const int per = c.physics == A3D_2ORDER ? 2 : 3;
+        for (int it = 0; it < c.nt; ++it)
+            for (int k = 0; k + 1 < per; ++k) {
+                float f = 0;
+                CUDA_TRY(cudaEventElapsedTime(&f, kev[per * it + k], kev[per * it + k + 1]));
+                kms[k] += f;
+                klaunch[k] += 1;
+            }
+    }
     if (ms) {
         float f = 0;
         CUDA_TRY(cudaEventElapsedTime(&f, ev0, ev1));
@@ -553,6 +582,23 @@ extern "C" int a3d_forward_host(const a3d_config *cfg, const float *vel, const f
         rc = a3d_engine_run(e, &shots[i], recs_host ? recs_host + i * nrec : nullptr, 0, 0, nullptr, nullptr);
     a3d_engine_destroy(e);
     return rc;
+}
+
+extern "C" int a3d_engine_set_profiling(a3d_engine *e, int on) {
+    if (!e) return fail(A3D_E_ARG, "null engine");
+    e->profiling = on != 0;
+    e->kms[0] = e->kms[1] = 0;
+    e->klaunch[0] = e->klaunch[1] = 0;
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_kernel_times(const a3d_engine *e, double *ms, long long *launches) {
+    if (!e) return fail(A3D_E_ARG, "null engine");
+    for (int k = 0; k < 2; ++k) {
+        if (ms) ms[k] = e->kms[k];
+        if (launches) launches[k] = e->klaunch[k];
+    }
+    return A3D_OK;
 }
 
 extern "C" const char *a3d_last_error(void) { return a3d::g_err.c_str(); }

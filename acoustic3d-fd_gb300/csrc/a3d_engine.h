@@ -65,6 +65,12 @@ struct a3d_engine {
     CUtensorMap mvel[9], mstr[12];
     int nvel = 0, nstr = 0;
 
+    // optional per-kernel timing: events around every launch of each kernel kind
+    bool profiling = false;
+    std::vector<cudaEvent_t> kev;  // 3 per step (1st order) or 2 per step (2nd order)
+    double kms[2] = {0, 0};        // summed device ms: [0] velocity / 2nd-order step, [1] stress
+    long long klaunch[2] = {0, 0};
+
     ~a3d_engine();
     void *dalloc(size_t bytes);  // zeroed; null on failure
     int run(const a3d_shot &s, float *rec_dev, const a3d::SnapHook *hook, double *ms);

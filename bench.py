@@ -1,0 +1,357 @@
+#!/usr/bin/env python
+"""Benchmark of the forward-modelling hot path: grid-point updates per second.
+
+Default workload (the configuration the headline metric is quoted on): the
+1st-order staggered-grid isotropic engine with density, 256^3 model, dx = 10 m,
+nt = 2000, dt = 0.4*dx/vmax (CFL 0.4), velocity = Gaussian-smoothed (sigma 8
+cells) N(0,1) noise from seed 2 mapped to 1500-4500 m/s, Gardner density
+rho = 310 v^0.25, 20-cell PML, 20 Hz Ricker at the grid centre, depth 8,
+receivers on every surface node.  FP32 wavefields.
+
+A "step" is one shot: the full nt-step time loop over the padded grid.
+  value  Gpts/s = updated cells of the padded grid x nt x shots / device time
+         (CUDA events on the engine's stream around each time loop; inputs resident)
+  e2e    the same metric through the host-buffer C-ABI call a3d_forward_host:
+         model H2D, time loop, record D2H, every step
+  roofline  the dominant kernel's algorithmic bytes per launch / its mean launch
+         time (events around every launch), against the measured HBM peak
+  cpu_baseline  the CPU restatement of the reference update (oracle, OpenMP, all
+         host cores) on a bounded sample of the same workload
+  rel_l2_vs_fp64  shot-record error of the FP32 run against the same shot run in
+         FP64 (GPU FP64 path), outside the timed region
+
+--impl reference runs the reference's update restated on the CPU (the reference
+itself is CUDA-only; its kernels' GPU timing is reported in the design doc).
+Multi-GPU: replicas (torchrun; each rank runs its own shots, no collective in the
+data path); value = all ranks' updates / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "acoustic3d-fd_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+# bytes per cell of the two isotropic sweeps as built (compulsory traffic of each launch):
+#   velocity sweep: read P, u, v, w, rho; write u, v, w            -> 8 words
+#   stress sweep:   read u, v, w, P, rho, vp; write P              -> 7 words
+# and the whole-step algorithmic figure of an unsplit formulation (u,v,w,P read and
+# written once + 2 parameters): 10 words = 40 B per cell update.
+KERNEL_BYTES = {"iso": (32.0, 28.0), "2o": (16.0, None), "vti": (40.0, 48.0), "tti": (56.0, 60.0)}
+STEP_BYTES = {"iso": 40.0, "2o": 16.0, "vti": 56.0, "tti": 60.0}
+
+
+def smooth_model(n, seed, lo, hi, sigma=8.0):
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    a = gaussian_filter(rng.standard_normal((n, n, n)).astype(np.float32), sigma=sigma, mode="reflect")
+    a = (a - a.min()) / (a.max() - a.min())
+    return (lo + (hi - lo) * a).astype(np.float32)
+
+
+def workload(name, nt_override=None):
+    if name == "iso256":
+        n, dx, vmax = 256, 10.0, 4500.0
+        vel = smooth_model(n, 2, 1500.0, vmax)
+        rho = (310.0 * vel.astype(np.float64) ** 0.25).astype(np.float32)
+        dt = np.float32(0.4 * dx / vmax)
+        nt = nt_override or 2000
+        cfg = dict(physics="iso", nx=n, ny=n, nz=n, dx=dx, dy=dx, dz=dx, nt=nt, dt=float(dt), fm=20.0,
+                   npml=20)
+        return cfg, {"vel": vel, "rho": rho}, (n // 2, n // 2, 8), \
+            dict(workload="iso1order_256cube_nt%d" % nt, model="256x256x256", dx_m=dx, nt=nt,
+                 dt_s=float(dt), npml=20, fm_hz=20.0, shot=[n // 2, n // 2, 8], storage="fp32")
+    if name == "2o128":
+        n, dx = 128, 10.0
+        z = np.arange(n)
+        col = np.where(z < 40, 1500.0, np.where(z < 85, 2500.0, 3500.0)).astype(np.float32)
+        vel = np.broadcast_to(col, (n, n, n)).copy()
+        nt = nt_override or 1000
+        cfg = dict(physics="2o", nx=n, ny=n, nz=n, dx=dx, dy=dx, dz=dx, nt=nt, dt=5e-4, fm=25.0, npml=50,
+                   rec_z=1)
+        return cfg, {"vel": vel}, (64, 64, 5), \
+            dict(workload="2order_128cube_3layer_nt%d" % nt, model="128x128x128", dx_m=dx, nt=nt, dt_s=5e-4,
+                 sponge=50, fm_hz=25.0, shot=[64, 64, 5], storage="fp32")
+    raise SystemExit(f"unknown workload {name}")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                rows.append((float(f[0]), float(f[1]), float(f[2]), f[3:7]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        load = [r for r in rows if r[2] > 300.0] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in load for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(load), "reasons": reasons}
+
+
+def cpu_rate(cfgd, models, shot, threads, nt_a=3, nt_b=9):
+    """Oracle (the reference update on the CPU, literal arithmetic) Gpts/s from two
+    runs of different length, so set-up time cancels."""
+    import oracle as O
+    eng = cfgd["physics"]
+    times = []
+    for nt in (nt_a, nt_b):
+        s = O.Shot(cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"], dz=cfgd["dz"],
+                   sx=shot[0], sy=shot[1], sz=shot[2], nt=nt, dt=cfgd["dt"], fm=cfgd["fm"],
+                   npml=cfgd["npml"], rec_z=cfgd.get("rec_z", 1), form=0, threads=threads)
+        t0 = time.perf_counter()
+        O.run(eng, s, models, "f32")
+        times.append(time.perf_counter() - t0)
+    pad = cfgd["npml"] + (4 if eng == "2o" else 0)
+    cells = (cfgd["nx"] + 2 * pad - 8) * (cfgd["ny"] + 2 * pad - 8) * (cfgd["nz"] + 2 * pad - 8)
+    dt = max(times[1] - times[0], 1e-9)
+    return cells * (nt_b - nt_a) / dt / 1e9, dict(steps=nt_b - nt_a, seconds=dt)
+
+
+def updated_cells(cfgd):
+    pad = cfgd["npml"] + (4 if cfgd["physics"] == "2o" else 0)
+    return (cfgd["nx"] + 2 * pad - 8) * (cfgd["ny"] + 2 * pad - 8) * (cfgd["nz"] + 2 * pad - 8)
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(workload_name):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(workload_name)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args, cfgd, models, shot, meta):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_rate(cfgd, models, shot, threads, 1, 2)
+    rates, secs = [], 0.0
+    for _ in range(args.steps):
+        r, info = cpu_rate(cfgd, models, shot, threads)
+        rates.append(r)
+        secs += info["seconds"]
+    value = float(np.mean(rates))
+    sample = f"{cfgd['physics']} {meta['model']} grid, 6 time steps per bench step (difference of 9- and 3-step runs)"
+    line = {"metric": "Gpts/s", "value": value, "unit": "Gpts/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": meta, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "Gpts/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="iso256", choices=["iso256", "2o128"])
+    ap.add_argument("--nt", type=int, default=0, help="override nt (profiling runs only)")
+    ap.add_argument("--tile-x", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error check")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+
+    cfgd, models, shot, meta = workload(args.workload, args.nt or None)
+    if args.impl == "reference":
+        run_reference(args, cfgd, models, shot, meta)
+        return
+
+    import a3d
+    import build as pkg_build
+    pkg_build.build()
+    ws, rank, local = dist_env()
+    dev = local
+    group = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(dev)
+        dist.init_process_group("nccl")
+        group = dist
+    eng = cfgd["physics"]
+    cfg = a3d.make_config(eng, cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"],
+                          dz=cfgd["dz"], nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
+                          rec_z=cfgd.get("rec_z", -1), tile_x=args.tile_x)
+    e = a3d.Engine(cfg, models, device=dev)
+    # replicas: rank r shifts its shot along x
+    sx = min(cfgd["nx"] - 1, shot[0] + 4 * rank)
+    for _ in range(args.warmup):
+        e.run_device(sx, shot[1], shot[2])
+
+    def barrier():
+        if group:
+            import torch
+            torch.cuda.synchronize(dev)
+            group.barrier()
+
+    # ---- timed region: K shots, inputs resident
+    barrier()
+    e.set_profiling(True)
+    dev_ms = 0.0
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            dev_ms += e.run_device(sx, shot[1], shot[2])
+        wall = time.perf_counter() - t0
+    barrier()
+    kms, kn = e.kernel_times()
+    e.set_profiling(False)
+    if group:
+        import torch
+        t = torch.tensor([dev_ms], dtype=torch.float64, device=f"cuda:{dev}")
+        group.all_reduce(t, op=group.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    cells = updated_cells(cfgd)
+    nt = cfgd["nt"]
+    value = cells * nt * args.steps * ws / (dev_ms / 1000.0) / 1e9
+    ms_per_step = dev_ms / args.steps
+
+    # ---- roofline of the dominant kernel
+    peak, peak_kind = measured_peak()
+    kb = KERNEL_BYTES[eng]
+    per = [kms[i] / kn[i] if kn[i] else 0.0 for i in range(2)]
+    dom = 0 if (per[0] >= per[1] or kb[1] is None) else 1
+    achieved = kb[dom] * cells / (per[dom] / 1000.0) / 1e9
+    step_gbs = STEP_BYTES[eng] * cells * nt * args.steps / (dev_ms / 1000.0) / 1e9
+    kname = {("iso", 0): "iso_vel", ("iso", 1): "iso_stress", ("2o", 0): "k2o_step"}.get((eng, dom), "?")
+    tr = traffic_per_launch(meta["workload"])
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": tr.get(kname) if isinstance(tr, dict) else None,
+                "peak_source": peak_kind, "bytes_per_cell": kb[dom],
+                "kernel_ms_per_launch": per[dom],
+                "step": {"bytes_per_cell": STEP_BYTES[eng], "achieved": step_gbs, "frac": step_gbs / peak}}
+
+    # ---- FP64 error of the FP32 record (outside the timed region)
+    rel = None
+    if not args.no_fp64 and rank == 0:
+        rec32 = e.run(sx, shot[1], shot[2])
+        cfg64 = a3d.make_config(eng, cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"],
+                                dz=cfgd["dz"], nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
+                                rec_z=cfgd.get("rec_z", -1), storage=a3d.FP64)
+        e64 = a3d.Engine(cfg64, models, device=dev)
+        rec64 = e64.run(sx, shot[1], shot[2])
+        e64.close()
+        d = np.linalg.norm((rec32.astype(np.float64) - rec64).ravel())
+        rel = float(d / np.linalg.norm(rec64.astype(np.float64).ravel()))
+    e.close()
+
+    # ---- e2e through the host-buffer C-ABI call (H2D model, loop, D2H record)
+    n_model = len(a3d.READS[cfg.physics])
+    pad = cfgd["npml"] + (4 if eng == "2o" else 0)
+    padded = (cfgd["nx"] + 2 * pad) * (cfgd["ny"] + 2 * pad) * ((cfgd["nz"] + 2 * pad + 7) // 8 * 8)
+    h2d = 4 * padded * n_model
+    d2h = 4 * cfgd["nx"] * cfgd["ny"] * cfgd["nt"]
+    a3d.forward_host(cfg, models, [(sx, shot[1], shot[2])], device=dev)  # warm
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        a3d.forward_host(cfg, models, [(sx, shot[1], shot[2])], device=dev)
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    e2e_val = cells * nt * args.e2e_steps * ws / e2e_s / 1e9
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        r, info = cpu_rate(cfgd, models, shot, threads)
+        cpu = {"value": r, "unit": "Gpts/s", "cores": threads, "kind": "port",
+               "sample": f"{meta['model']} grid, {info['steps']} time steps (difference of 9- and 3-step "
+                         f"runs of the oracle, literal arithmetic), {info['seconds']:.1f} s"}
+
+    if rank == 0:
+        clocks = clk.summary()
+        line = {"metric": "Gpts/s", "value": value, "unit": "Gpts/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": dict(meta, parallelism=f"replicas{ws}",
+                               l2="inputs larger than L2: %d MB of wavefields and model" %
+                                  (4 * padded * (7 if eng == 'iso' else 3) // 2**20),
+                               tile_x=args.tile_x or 8),
+                "shots_per_hour": 3600.0 * 1000.0 / ms_per_step * ws,
+                "rel_l2_vs_fp64": rel,
+                "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": {"value": e2e_val, "unit": "Gpts/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "call": "a3d_forward_host"},
+                "wall_s_timed": wall, "clocks": clocks,
+                "gpu_launches": int(kn[0] + kn[1])}
+        print(json.dumps(line), flush=True)
+    if group:
+        group.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -142,6 +142,13 @@ int a3d_forward_host(const a3d_config *cfg, const float *vel, const float *rho, 
                      const float *del, const float *theta, const float *phi,
                      const a3d_shot *shots, int nshot, float *recs_host, int device);
 
+/* Per-kernel device timing (CUDA events around every launch, on the engine's
+ * stream).  After runs with profiling on, ms[0]/launches[0] sum the velocity
+ * sweeps (1st order) or the fused steps (2nd order), ms[1]/launches[1] the stress
+ * sweeps.  Turning profiling on resets the sums. */
+int a3d_engine_set_profiling(a3d_engine *e, int on);
+int a3d_engine_kernel_times(const a3d_engine *e, double *ms, long long *launches);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char *a3d_last_error(void);
 
