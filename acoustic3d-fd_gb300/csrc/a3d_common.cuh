@@ -165,15 +165,19 @@ __device__ __forceinline__ void consumer_sync(int nthreads) {
 }
 
 // ---------------------------------------------------------------------------
-// work split: the (tile, plane) space of a sweep, linearised as
-//     w = tile * NY + (y - y_begin),   tile = tz + ntz * tx
-// and cut into gridDim.x contiguous ranges of nearly equal length, so every CTA
-// gets the same number of output planes whatever the tile count.
+// work split: the (tile, plane) space of a sweep is cut along y into chunks of
+// Yc planes (the last one may be shorter) and linearised chunk-major:
+//     w = c * (ntiles * Yc) + tile * len_c + (y - y_begin - c * Yc),
+//     tile = tz + ntz * tx,  len_c = planes of chunk c,
+// then split into gridDim.x contiguous ranges of nearly equal length.  With one
+// chunk-segment per CTA (the host picks Yc so), CTAs that run concurrently march
+// the same y range and neighbouring tiles read each other's halos from L2.
 
 struct Sweep {
     int ntz, ntx;    // tiles along z and x
     int y_begin;     // first output plane
     int NY;          // output planes per tile
+    int Yc;          // planes per y chunk
     long long W;     // ntz * ntx * NY
 };
 

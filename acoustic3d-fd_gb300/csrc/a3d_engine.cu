@@ -35,11 +35,20 @@ void clear_error() { g_err.clear(); }
     } while (0)
 
 static int g_sms = 0;
-int occ_grid(int occ, long long W) {
-    long long g = (long long)(g_sms > 0 ? g_sms : 148) * (occ > 0 ? occ : 1);
-    long long cap = W / 24;
-    if (cap < 1) cap = 1;
-    return (int)(g < cap ? g : cap);
+int plan_sweep(Sweep &sw, int occ) {
+    const long long slots = (long long)(g_sms > 0 ? g_sms : 148) * (occ > 0 ? occ : 1);
+    const long long ntiles = (long long)sw.ntz * sw.ntx;
+    sw.W = ntiles * sw.NY;
+    if (ntiles <= slots) {
+        long long C = slots / ntiles;
+        const long long cmax = sw.NY / 16 > 1 ? sw.NY / 16 : 1;
+        if (C > cmax) C = cmax;
+        sw.Yc = (int)((sw.NY + C - 1) / C);
+        C = (sw.NY + sw.Yc - 1) / sw.Yc;
+        return (int)(ntiles * C);
+    }
+    sw.Yc = sw.NY;
+    return (int)slots;
 }
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -68,7 +77,7 @@ static int make_map(CUtensorMap *m, const void *base, bool f64, const Grid &g, i
     CUresult r = enc(m, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                      const_cast<void *>(base), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                     CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(A3D_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return A3D_OK;
 }
@@ -115,13 +124,22 @@ void *a3d_engine::dalloc(size_t bytes) {
     return p;
 }
 
-static int upload_model(a3d_engine *e, const float *m, float **dst, std::vector<float> &tmp) {
-    const Grid &g = e->g;
-    pad_model(m, g, tmp.data());
-    *dst = (float *)e->dalloc(g.elems() * 4);
-    if (!*dst) return fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", g.elems() * 4);
-    CUDA_TRY(cudaMemcpy(*dst, tmp.data(), g.elems() * 4, cudaMemcpyHostToDevice));
+void *a3d_engine::dfield(size_t es) {
+    char *p = (char *)dalloc(g.elems() * es);
+    return p ? p + Grid::zoff * es : nullptr;
+}
+
+// copy a host image of a float field allocation (elems() floats) into a new field
+static int upload_image(a3d_engine *e, const std::vector<float> &img, float **dst) {
+    *dst = (float *)e->dfield(4);
+    if (!*dst) return fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", e->field_bytes(4));
+    CUDA_TRY(cudaMemcpy(e->field_alloc(*dst, 4), img.data(), e->field_bytes(4), cudaMemcpyHostToDevice));
     return A3D_OK;
+}
+
+static int upload_model(a3d_engine *e, const float *m, float **dst, std::vector<float> &tmp) {
+    pad_model(m, e->g, tmp.data());
+    return upload_image(e, tmp, dst);
 }
 
 static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const float *eps,
@@ -131,7 +149,7 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     std::vector<float> tmp(g.elems());
     const size_t fb = g.elems() * e->esz;
     auto field = [&](void **p) -> int {
-        *p = e->dalloc(fb);
+        *p = e->dfield(e->esz);
         return *p ? A3D_OK : fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", fb);
     };
     int rc;
@@ -147,9 +165,7 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
             const float t = tmp[i] * c.dt;
             tmp[i] = t * t;
         }
-        e->vv = (float *)e->dalloc(g.elems() * 4);
-        if (!e->vv) return fail(A3D_E_NOMEM, "device allocation failed");
-        CUDA_TRY(cudaMemcpy(e->vv, tmp.data(), g.elems() * 4, cudaMemcpyHostToDevice));
+        if ((rc = upload_image(e, tmp, &e->vv))) return rc;
         e->v_mute = (size_t)c.nx * c.ny * c.nz > 1 ? vel[1] : vel[0];  // 2O:403
         if ((rc = field(&e->X)) || (rc = field(&e->Y))) return rc;
         // sponge factors per axis
@@ -188,9 +204,7 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
         for (int k = 0; k < 4; ++k) {
             pad_model(k < 2 ? theta : phi, g, ang.data());
             for (size_t i = 0; i < ang.size(); ++i) tmp[i] = (k % 2 == 0) ? cosf(ang[i]) : sinf(ang[i]);
-            *dst[k] = (float *)e->dalloc(g.elems() * 4);
-            if (!*dst[k]) return fail(A3D_E_NOMEM, "device allocation failed");
-            CUDA_TRY(cudaMemcpy(*dst[k], tmp.data(), g.elems() * 4, cudaMemcpyHostToDevice));
+            if ((rc = upload_image(e, tmp, dst[k]))) return rc;
         }
     }
     // mute velocity: the padded model's element 1, i.e. model cell (0,0,0) (..iso..:340)
@@ -353,8 +367,8 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
     };
     int rc;
     if (c.physics == A3D_2ORDER) {
-        CUDA_TRY(cudaMemsetAsync(X, 0, fb, st));
-        CUDA_TRY(cudaMemsetAsync(Y, 0, fb, st));
+        CUDA_TRY(cudaMemsetAsync(field_alloc(X, esz), 0, fb, st));
+        CUDA_TRY(cudaMemsetAsync(field_alloc(Y, esz), 0, fb, st));
         const int pad = g.pad;
         const int sxp = s.sx + pad, syp = s.sy + pad, szp = s.sz + pad;
         // step 0's dipole into the zero current level (2O:443)
@@ -404,7 +418,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
     } else {
         void *fields[11] = {u, v, w, P, Q, px, py, pz, qx, qy, qz};
         for (void *f : fields)
-            if (f) CUDA_TRY(cudaMemsetAsync(f, 0, fb, st));
+            if (f) CUDA_TRY(cudaMemsetAsync(field_alloc(f, esz), 0, fb, st));
         const int np = npml;
         K1Launch Lv{}, Ls{};
         K1Params p{};

@@ -73,5 +73,8 @@ struct a3d_engine {
 
     ~a3d_engine();
     void *dalloc(size_t bytes);  // zeroed; null on failure
+    void *dfield(size_t esz);    // zeroed padded field; returns its base (allocation + zoff)
+    size_t field_bytes(size_t esz) const { return g.elems() * esz; }
+    void *field_alloc(void *base, size_t es) const { return (char *)base - a3d::Grid::zoff * es; }
     int run(const a3d_shot &s, float *rec_dev, const a3d::SnapHook *hook, double *ms);
 };

@@ -47,22 +47,23 @@ static cudaError_t k1_launch(Kern kern, int nthreads, size_t smem, long long W, 
         if (e != cudaSuccess) return e;
         attr_done = true;
     }
-    if (grid <= 0) {
-        int occ = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nthreads, smem);
-        grid = occ_grid(occ, W);
-    }
+    (void)W;
     kern<<<grid, nthreads, smem, st>>>(args...);
     return cudaGetLastError();
 }
 
-template <int TX>
-static void k1_sweep(K1Params &p) {
+// sweep of the updated region [4, nn-4)^3 in 32 x TX tiles; returns gridDim.x
+template <int TX, class Kern>
+static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid) {
     p.sw.ntz = (p.nnz - 2 * MM + 31) / 32;
     p.sw.ntx = (p.nnx - 2 * MM + TX - 1) / TX;
     p.sw.y_begin = MM;
     p.sw.NY = p.nny - 2 * MM;
-    p.sw.W = (long long)p.sw.ntz * p.sw.ntx * p.sw.NY;
+    int occ = 0;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nthreads, smem);
+    const int g = plan_sweep(p.sw, occ);
+    return grid > 0 ? grid : g;
 }
 
 // loads of a stored field value / smem tile element as the arithmetic type

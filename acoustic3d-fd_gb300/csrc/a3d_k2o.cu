@@ -18,6 +18,7 @@
 //   record = sponge(X) at the receivers          cuda_record on p0 after absorb
 // so the only HBM traffic is X and Y read, vv read, Y written: 16 B per cell.
 #include "a3d_kernels.cuh"
+#include "a3d_pipe.cuh"
 
 namespace a3d {
 
@@ -28,183 +29,121 @@ struct K2OSmem {
     static constexpr int AW = 40, AH = TX + 8;  // A tile: [AH][AW]
     static constexpr int A_ELEMS = AW * AH;
     static constexpr int B_ELEMS = 32 * TX;
-    static constexpr size_t A_BYTES = (size_t)A_ELEMS * sizeof(S);
-    static constexpr size_t B_BYTES = (size_t)B_ELEMS * sizeof(S);
-    static constexpr size_t VV_BYTES = (size_t)B_ELEMS * sizeof(float);
+    static constexpr uint32_t A_BYTES = (uint32_t)(A_ELEMS * sizeof(S));
+    static constexpr uint32_t B_BYTES = (uint32_t)(B_ELEMS * sizeof(S));
+    static constexpr uint32_t VV_BYTES = (uint32_t)(B_ELEMS * sizeof(float));
     static constexpr size_t A_STRIDE = (A_BYTES + 127) / 128 * 128;
     static constexpr size_t B_STRIDE = (B_BYTES + VV_BYTES + 127) / 128 * 128;
     static constexpr size_t BAR_OFF = KA * A_STRIDE + KB * B_STRIDE;
-    static constexpr size_t TOTAL = BAR_OFF + (2 * KA + 2 * KB) * 8 + 16;
+    static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBars<KA, KB>);
 };
 
 template <int TX, class S>
 __global__ void __launch_bounds__(32 * TX + 32)
     k2o_step(const __grid_constant__ CUtensorMap tm_cur, const __grid_constant__ CUtensorMap tm_prev,
-             const __grid_constant__ CUtensorMap tm_vv, S *__restrict__ ybuf, K2OParams p) {
+             const __grid_constant__ CUtensorMap tm_vv, S *__restrict__ ybuf,
+             const __grid_constant__ K2OParams p) {
     using L = K2OSmem<TX, S>;
     using T = typename Arith<S>::T;
     constexpr int NC = 32 * TX;  // consumer threads
     extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t *fullA = reinterpret_cast<uint64_t *>(smem + L::BAR_OFF);
-    uint64_t *emptyA = fullA + L::KA;
-    uint64_t *fullB = emptyA + L::KA;
-    uint64_t *emptyB = fullB + L::KB;
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(emptyB + L::KB);
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < L::KA; ++i) { mbar_init(&fullA[i], 1); mbar_init(&emptyA[i], NC); }
-        for (int i = 0; i < L::KB; ++i) { mbar_init(&fullB[i], 1); mbar_init(&emptyB[i], NC); }
-        *abort_flag = 0;
-        fence_mbar_init();
-    }
+    auto &bars = *reinterpret_cast<PipeBars<L::KA, L::KB> *>(smem + L::BAR_OFF);
+    unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
+    if (threadIdx.x == 0) bars.init(NC);
     __syncthreads();
-
     long long w0, w1;
     cta_range(p.sw, w0, w1);
     if (w0 >= w1) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (warp == TX) {
-        // ------------------------------------------------------------ producer
         if (lane != 0) return;
         prefetch_tmap(&tm_cur);
         prefetch_tmap(&tm_prev);
         prefetch_tmap(&tm_vv);
-        long long ja = 0, jb = 0;  // A and B item counters
-        bool ok = true;
-        for (long long w = w0; w < w1 && ok;) {
-            const int tile = (int)(w / p.sw.NY);
-            const int ya = p.sw.y_begin + (int)(w % p.sw.NY);
-            long long wend = (long long)(tile + 1) * p.sw.NY;
-            if (wend > w1) wend = w1;
-            const int yb = ya + (int)(wend - w);
-            const int z0 = MM + 32 * (tile % p.sw.ntz), x0 = MM + TX * (tile / p.sw.ntz);
-            for (int q = ya - MM; q < yb + MM && ok; ++q, ++ja) {
-                const int sa = (int)(ja % L::KA);
-                if (ja >= L::KA)
-                    ok = mbar_wait(&emptyA[sa], (uint32_t)(((ja / L::KA) - 1) & 1), p.err,
-                                   KERR_EMPTY_TIMEOUT, abort_flag);
-                if (!ok) break;
-                mbar_arrive_expect_tx(&fullA[sa], (uint32_t)L::A_BYTES);
-                tma_load_3d(smem + sa * L::A_STRIDE, &tm_cur, &fullA[sa], z0 - MM, x0 - MM, q);
-                const int o = q - MM;
-                if (o >= ya) {
-                    const int sb = (int)(jb % L::KB);
-                    if (jb >= L::KB)
-                        ok = mbar_wait(&emptyB[sb], (uint32_t)(((jb / L::KB) - 1) & 1), p.err,
-                                       KERR_EMPTY_TIMEOUT, abort_flag);
-                    if (!ok) break;
-                    unsigned char *bst = smem + L::KA * L::A_STRIDE + sb * L::B_STRIDE;
-                    mbar_arrive_expect_tx(&fullB[sb], (uint32_t)(L::B_BYTES + L::VV_BYTES));
-                    tma_load_3d(bst, &tm_prev, &fullB[sb], z0, x0, o);
-                    tma_load_3d(bst + L::B_BYTES, &tm_vv, &fullB[sb], z0, x0, o);
-                    ++jb;
-                }
-            }
-            w = wend;
-        }
-        // drain: wait until every issued copy has landed before the CTA may exit
-        for (long long j = (ja > L::KA ? ja - L::KA : 0); j < ja; ++j)
-            if (!mbar_wait(&fullA[j % L::KA], (uint32_t)((j / L::KA) & 1), p.err,
-                           KERR_DRAIN_TIMEOUT, abort_flag))
-                break;
-        for (long long j = (jb > L::KB ? jb - L::KB : 0); j < jb; ++j)
-            if (!mbar_wait(&fullB[j % L::KB], (uint32_t)((j / L::KB) & 1), p.err,
-                           KERR_DRAIN_TIMEOUT, abort_flag))
-                break;
+        pipe_produce<TX, L::KA, L::KB>(
+            p.sw, w0, w1, bars, ringA, L::A_STRIDE, L::A_BYTES, ringB, L::B_STRIDE,
+            L::B_BYTES + L::VV_BYTES, p.err,
+            [&](unsigned char *dst, uint64_t *bar, const Seg &s, int q) {
+                tma_load_3d(dst, &tm_cur, bar, s.z0 - MM, s.x0 - MM, q);
+            },
+            [&](unsigned char *dst, uint64_t *bar, const Seg &s, int o) {
+                tma_load_3d(dst, &tm_prev, bar, s.z0, s.x0, o);
+                tma_load_3d(dst + L::B_BYTES, &tm_vv, bar, s.z0, s.x0, o);
+            });
         return;
     }
 
-    // ---------------------------------------------------------------- consumers
     const int tx = warp, tz = lane;
     T win[9];  // current level at planes q-8 .. q (own column)
 #pragma unroll
     for (int i = 0; i < 9; ++i) win[i] = T(0);
-    long long ja = 0, jb = 0;
-    const T k0 = (T)S8_0, k1 = (T)S8_1, k2 = (T)S8_2, k3 = (T)S8_3, k4 = (T)S8_4;
-    for (long long w = w0; w < w1;) {
-        const int tile = (int)(w / p.sw.NY);
-        const int ya = p.sw.y_begin + (int)(w % p.sw.NY);
-        long long wend = (long long)(tile + 1) * p.sw.NY;
-        if (wend > w1) wend = w1;
-        const int yb = ya + (int)(wend - w);
-        const int z0 = MM + 32 * (tile % p.sw.ntz), x0 = MM + TX * (tile / p.sw.ntz);
-        const int iz = z0 + tz, ix = x0 + tx;
-        const bool active = iz < p.nnz - MM && ix < p.nnx - MM;
-        // sponge factors of this column (hi == 0: no sponge on that face)
-        const float2 fz = p.fz[min(iz, p.nnz - 1)], fx = p.fx[min(ix, p.nnx - 1)];
-        const bool rec_row = iz == p.gz && ix >= p.rx0 && ix < p.rx0 + p.nx;
-        for (int q = ya - MM; q < yb + MM; ++q, ++ja) {
-            const int sa = (int)(ja % L::KA);
-            if (!mbar_wait(&fullA[sa], (uint32_t)((ja / L::KA) & 1), p.err, KERR_FULL_TIMEOUT,
-                           abort_flag))
-                return;
-            const S *At = reinterpret_cast<const S *>(smem + sa * L::A_STRIDE);
+    int iz = 0, ix = 0;
+    bool active = false, rec_row = false;
+    float2 fz{0.f, 0.f}, fx{0.f, 0.f};
+    const T k1 = (T)S8_1, k2 = (T)S8_2, k3 = (T)S8_3, k4 = (T)S8_4;
+    pipe_consume<TX, L::KA, L::KB>(
+        p.sw, w0, w1, bars, ringA, L::A_STRIDE, ringB, L::B_STRIDE, p.err,
+        [&](const Seg &s) {
+            iz = s.z0 + tz;
+            ix = s.x0 + tx;
+            active = iz < p.nnz - MM && ix < p.nnx - MM;
+            // sponge factors of this column (hi == 0: no sponge on that face)
+            fz = p.fz[min(iz, p.nnz - 1)];
+            fx = p.fx[min(ix, p.nnx - 1)];
+            rec_row = iz == p.gz && ix >= p.rx0 && ix < p.rx0 + p.nx;
+        },
+        [&](unsigned char *st, const Seg &, int) {
+            const S *At = reinterpret_cast<const S *>(st);
 #pragma unroll
             for (int i = 0; i < 8; ++i) win[i] = win[i + 1];
             win[8] = (T)At[(tx + MM) * L::AW + tz + MM];
-            const int o = q - MM;
-            if (o >= ya) {
-                const int sb = (int)(jb % L::KB);
-                if (!mbar_wait(&fullB[sb], (uint32_t)((jb / L::KB) & 1), p.err,
-                               KERR_FULL_TIMEOUT, abort_flag))
-                    return;
-                // the halo'd tile of plane o was loaded 4 items ago
-                const S *Ao = reinterpret_cast<const S *>(smem + ((ja - MM) % L::KA) * L::A_STRIDE);
-                const unsigned char *bst = smem + L::KA * L::A_STRIDE + sb * L::B_STRIDE;
-                const S *Bp = reinterpret_cast<const S *>(bst);
-                const float *Bv = reinterpret_cast<const float *>(bst + L::B_BYTES);
-                if (active) {
-                    const int c = (tx + MM) * L::AW + tz + MM;
-                    const T cur = win[4];
-                    T c1 = k0 * cur, c2 = c1, c3 = c1;
-                    // z, x from the tile; y from the register window (2O:284-289)
-                    c1 = fma_t(k1, (T)Ao[c - 1] + (T)Ao[c + 1], c1);
-                    c2 = fma_t(k1, (T)Ao[c - L::AW] + (T)Ao[c + L::AW], c2);
-                    c3 = fma_t(k1, win[5] + win[3], c3);
-                    c1 = fma_t(k2, (T)Ao[c - 2] + (T)Ao[c + 2], c1);
-                    c2 = fma_t(k2, (T)Ao[c - 2 * L::AW] + (T)Ao[c + 2 * L::AW], c2);
-                    c3 = fma_t(k2, win[6] + win[2], c3);
-                    c1 = fma_t(k3, (T)Ao[c - 3] + (T)Ao[c + 3], c1);
-                    c2 = fma_t(k3, (T)Ao[c - 3 * L::AW] + (T)Ao[c + 3 * L::AW], c2);
-                    c3 = fma_t(k3, win[7] + win[1], c3);
-                    c1 = fma_t(k4, (T)Ao[c - 4] + (T)Ao[c + 4], c1);
-                    c2 = fma_t(k4, (T)Ao[c - 4 * L::AW] + (T)Ao[c + 4 * L::AW], c2);
-                    c3 = fma_t(k4, win[8] + win[0], c3);
-                    c1 *= (T)p.dz2;
-                    c2 *= (T)p.dx2;
-                    c3 *= (T)p.dy2;
-                    const int bi = tx * 32 + tz;
-                    const T m = (T)Bv[bi] * ((c1 + c2) + c3);
-                    const float2 fy = p.fy[o];
-                    const T prev = sponge3<T>((T)Bp[bi], fy, fx, fz);
-                    T nxt;
-                    if constexpr (sizeof(T) == 4)
-                        nxt = upd2o(cur, prev, m);
-                    else
-                        nxt = (T(2) * cur - prev) + m;
-                    nxt = sponge3<T>(nxt, fy, fx, fz);
-                    if (ix == p.s_x && o == p.s_y) {  // next step's dipole (2O:184-185)
-                        if (iz == p.s_z) nxt = nxt + (T)p.w_next;
-                        if (iz == p.s_z + 2) nxt = nxt - (T)p.w_next;
-                    }
-                    const size_t g = (size_t)iz + (size_t)p.ldz * ((size_t)ix + (size_t)p.nnx * o);
-                    ybuf[g] = to_store<S, T>(nxt);
-                    if (rec_row && o >= p.ry0 && o < p.ry0 + p.ny) {
-                        const int rx = ix - p.rx0, ry = o - p.ry0;
-                        const size_t tr = (size_t)rx + (size_t)p.nx * ry;
-                        T r = sponge3<T>(cur, fy, fx, fz);
-                        if (p.mute_nt && p.it < p.mute_nt[tr]) r = T(0);
-                        p.rec[tr * p.nt + p.it] = (float)r;
-                    }
-                }
-                mbar_arrive(&emptyB[sb]);
-                ++jb;
+        },
+        [&](unsigned char *sa, unsigned char *sb, const Seg &, int o) {
+            if (!active) return;
+            const S *Ao = reinterpret_cast<const S *>(sa);
+            const S *Bp = reinterpret_cast<const S *>(sb);
+            const float *Bv = reinterpret_cast<const float *>(sb + L::B_BYTES);
+            const float2 fy = p.fy[o];
+            const int c = (tx + MM) * L::AW + tz + MM, bi = tx * 32 + tz;
+            const T cur = win[4];
+            T c1 = (T)S8_0 * cur, c2 = c1, c3 = c1;
+            // z, x from the tile; y from the register window (2O:284-289)
+            c1 = fma_t(k1, (T)Ao[c - 1] + (T)Ao[c + 1], c1);
+            c2 = fma_t(k1, (T)Ao[c - L::AW] + (T)Ao[c + L::AW], c2);
+            c3 = fma_t(k1, win[5] + win[3], c3);
+            c1 = fma_t(k2, (T)Ao[c - 2] + (T)Ao[c + 2], c1);
+            c2 = fma_t(k2, (T)Ao[c - 2 * L::AW] + (T)Ao[c + 2 * L::AW], c2);
+            c3 = fma_t(k2, win[6] + win[2], c3);
+            c1 = fma_t(k3, (T)Ao[c - 3] + (T)Ao[c + 3], c1);
+            c2 = fma_t(k3, (T)Ao[c - 3 * L::AW] + (T)Ao[c + 3 * L::AW], c2);
+            c3 = fma_t(k3, win[7] + win[1], c3);
+            c1 = fma_t(k4, (T)Ao[c - 4] + (T)Ao[c + 4], c1);
+            c2 = fma_t(k4, (T)Ao[c - 4 * L::AW] + (T)Ao[c + 4 * L::AW], c2);
+            c3 = fma_t(k4, win[8] + win[0], c3);
+            c1 *= (T)p.dz2;
+            c2 *= (T)p.dx2;
+            c3 *= (T)p.dy2;
+            const T m = (T)Bv[bi] * ((c1 + c2) + c3);
+            const T prev = sponge3<T>((T)Bp[bi], fy, fx, fz);
+            T nxt;
+            if constexpr (sizeof(T) == 4)
+                nxt = upd2o(cur, prev, m);
+            else
+                nxt = (T(2) * cur - prev) + m;
+            nxt = sponge3<T>(nxt, fy, fx, fz);
+            if (ix == p.s_x && o == p.s_y) {  // next step's dipole (2O:184-185)
+                if (iz == p.s_z) nxt = nxt + (T)p.w_next;
+                if (iz == p.s_z + 2) nxt = nxt - (T)p.w_next;
             }
-            if (ja >= MM) mbar_arrive(&emptyA[(ja - MM) % L::KA]);
-        }
-        w = wend;
-    }
+            ybuf[(size_t)iz + (size_t)p.ldz * ((size_t)ix + (size_t)p.nnx * o)] = to_store<S, T>(nxt);
+            if (rec_row && o >= p.ry0 && o < p.ry0 + p.ny) {  // cuda_record after absorb (2O:452)
+                const size_t tr = (size_t)(ix - p.rx0) + (size_t)p.nx * (o - p.ry0);
+                T r = sponge3<T>(cur, fy, fx, fz);
+                if (p.mute_nt && p.it < p.mute_nt[tr]) r = T(0);
+                p.rec[tr * p.nt + p.it] = (float)r;
+            }
+        });
 }
 
 // ---------------------------------------------------------------------------
@@ -226,13 +165,10 @@ static cudaError_t launch_k2o_t(const K2OLaunch &L, cudaStream_t st) {
     p.sw.ntx = (p.nnx - 2 * MM + TX - 1) / TX;
     p.sw.y_begin = MM;
     p.sw.NY = p.nny - 2 * MM;
-    p.sw.W = (long long)p.sw.ntz * p.sw.ntx * p.sw.NY;
-    int grid = L.grid;
-    if (grid <= 0) {
-        int occ = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * TX + 32, SM::TOTAL);
-        grid = occ_grid(occ, p.sw.W);
-    }
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * TX + 32, SM::TOTAL);
+    int grid = plan_sweep(p.sw, occ);
+    if (L.grid > 0) grid = L.grid;
     kern<<<grid, 32 * TX + 32, SM::TOTAL, st>>>(L.tm_cur, L.tm_prev, L.tm_vv,
                                                 reinterpret_cast<S *>(L.ybuf), p);
     return cudaGetLastError();

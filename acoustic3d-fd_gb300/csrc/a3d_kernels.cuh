@@ -61,8 +61,10 @@ struct K2OLaunch {
 cudaError_t launch_k2o(const K2OLaunch &L, cudaStream_t st);
 size_t k2o_smem_bytes(int tx, bool fp64);
 
-// CTAs for a sweep of W plane-units: one full wave at the given occupancy, but
-// at least ~24 output planes per CTA so the 8-plane warm-up stays cheap
-int occ_grid(int occ_per_sm, long long W);
+// Pick gridDim.x and the y-chunk length of a sweep (ntz, ntx, NY already set)
+// for occ_per_sm resident CTAs per SM: if every tile fits in one wave, one CTA
+// per (tile, chunk) with as many chunks as the wave holds (each >= 16 planes);
+// otherwise one wave of CTAs over whole-y segments.  Fills sw.Yc and sw.W.
+int plan_sweep(Sweep &sw, int occ_per_sm);
 
 }  // namespace a3d

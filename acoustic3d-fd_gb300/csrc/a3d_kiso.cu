@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(32 * TX + 32)
 // iso_stress: maps {v (core), u (box HX), w (box HZ), P (core), rho, vp (core, float)}
 template <int TX, class S>
 struct IsoStrL {
-    static constexpr int KA = 8, KB = 3;
+    static constexpr int KA = 8, KB = 4;
     static constexpr uint32_t C = 32 * TX;
     static constexpr uint32_t UX = 32 * (TX + 8), WZ = 40 * TX;
     static constexpr uint32_t A_BYTES = C * sizeof(S);
@@ -243,49 +243,21 @@ __global__ void __launch_bounds__(32 * TX + 32)
 template <int TX, class S>
 static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
-    p.sw.ntz = (p.nnz - 2 * MM + 31) / 32;
-    p.sw.ntx = (p.nnx - 2 * MM + TX - 1) / TX;
-    p.sw.y_begin = MM;
-    p.sw.NY = p.nny - 2 * MM;
-    p.sw.W = (long long)p.sw.ntz * p.sw.ntx * p.sw.NY;
     if (L.kind == K1_ISO_VEL) {
-        using SM = IsoVelL<TX, S>;
-        auto kern = iso_vel<TX, S>;
         static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM::TOTAL);
-            if (e != cudaSuccess) return e;
-            attr = true;
-        }
         Maps<5> mp;
         for (int i = 0; i < 5; ++i) mp.m[i] = L.maps[i];
-        int grid = L.grid;
-        if (grid <= 0) {
-            int occ = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * TX + 32, SM::TOTAL);
-            grid = occ_grid(occ, p.sw.W);
-        }
-        kern<<<grid, 32 * TX + 32, SM::TOTAL, st>>>(mp, (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
-    } else {
-        using SM = IsoStrL<TX, S>;
-        auto kern = iso_stress<TX, S>;
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM::TOTAL);
-            if (e != cudaSuccess) return e;
-            attr = true;
-        }
-        Maps<6> mp;
-        for (int i = 0; i < 6; ++i) mp.m[i] = L.maps[i];
-        int grid = L.grid;
-        if (grid <= 0) {
-            int occ = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * TX + 32, SM::TOTAL);
-            grid = occ_grid(occ, p.sw.W);
-        }
-        kern<<<grid, 32 * TX + 32, SM::TOTAL, st>>>(mp, (S *)L.out0, p);
+        auto kern = iso_vel<TX, S>;
+        const int grid = k1_sweep<TX>(p, kern, 32 * TX + 32, IsoVelL<TX, S>::TOTAL, L.grid);
+        return k1_launch(kern, 32 * TX + 32, IsoVelL<TX, S>::TOTAL, p.sw.W, grid, st, attr, mp,
+                         (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
-    return cudaGetLastError();
+    static bool attr = false;
+    Maps<6> mp;
+    for (int i = 0; i < 6; ++i) mp.m[i] = L.maps[i];
+    auto kern = iso_stress<TX, S>;
+    const int grid = k1_sweep<TX>(p, kern, 32 * TX + 32, IsoStrL<TX, S>::TOTAL, L.grid);
+    return k1_launch(kern, 32 * TX + 32, IsoStrL<TX, S>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, p);
 }
 
 cudaError_t launch_iso(const K1Launch &L, cudaStream_t st) {

@@ -14,7 +14,7 @@ namespace a3d {
 // tti_vel: maps {P (H), Q (H), u, v, w (core), ct, st, cp, sp (core float)}
 template <int TX, class S>
 struct TtiVelL {
-    static constexpr int KA = 8, KB = 3;
+    static constexpr int KA = 8, KB = 4;
     static constexpr int AW = 40, AH = TX + 8;
     static constexpr uint32_t C = 32 * TX, H = AW * AH;
     static constexpr uint32_t A_BYTES = 2 * H * sizeof(S);
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(32 * TX + 32)
 // tti_stress: maps {u, v, w (H), P, Q (core), vp, eps, del, ct, st, cp, sp (core float)}
 template <int TX, class S>
 struct TtiStrL {
-    static constexpr int KA = 7, KB = 3;
+    static constexpr int KA = 8, KB = 4;
     static constexpr int AW = 40, AH = TX + 8;
     static constexpr uint32_t C = 32 * TX, H = AW * AH;
     static constexpr uint32_t A_BYTES = 3 * H * sizeof(S);
@@ -274,18 +274,19 @@ __global__ void __launch_bounds__(32 * TX + 32)
 template <int TX, class S>
 static cudaError_t launch_tti_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
-    k1_sweep<TX>(p);
     if (L.kind == K1_TTI_VEL) {
         static bool attr = false;
         Maps<9> mp;
         for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
-        return k1_launch(tti_vel<TX, S>, 32 * TX + 32, TtiVelL<TX, S>::TOTAL, p.sw.W, L.grid, st, attr,
+        const int grid = k1_sweep<TX>(p, tti_vel<TX, S>, 32 * TX + 32, TtiVelL<TX, S>::TOTAL, L.grid);
+        return k1_launch(tti_vel<TX, S>, 32 * TX + 32, TtiVelL<TX, S>::TOTAL, p.sw.W, grid, st, attr,
                          mp, (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
     static bool attr = false;
     Maps<12> mp;
     for (int i = 0; i < 12; ++i) mp.m[i] = L.maps[i];
-    return k1_launch(tti_stress<TX, S>, 32 * TX + 32, TtiStrL<TX, S>::TOTAL, p.sw.W, L.grid, st, attr,
+    const int grid = k1_sweep<TX>(p, tti_stress<TX, S>, 32 * TX + 32, TtiStrL<TX, S>::TOTAL, L.grid);
+    return k1_launch(tti_stress<TX, S>, 32 * TX + 32, TtiStrL<TX, S>::TOTAL, p.sw.W, grid, st, attr,
                      mp, (S *)L.out0, (S *)L.out1, p);
 }
 

@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(32 * TX + 32)
 // vti_stress: maps {v (core), u (HX), w (HZ), P, Q (core), rho, vp, eps, del (core float)}
 template <int TX, class S>
 struct VtiStrL {
-    static constexpr int KA = 8, KB = 3;
+    static constexpr int KA = 8, KB = 4;
     static constexpr uint32_t C = 32 * TX, UX = 32 * (TX + 8), WZ = 40 * TX;
     static constexpr uint32_t A_BYTES = C * sizeof(S);
     static constexpr uint32_t B_BYTES = (UX + WZ + 2 * C) * sizeof(S) + 4 * C * 4;
@@ -262,18 +262,19 @@ __global__ void __launch_bounds__(32 * TX + 32)
 template <int TX, class S>
 static cudaError_t launch_vti_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
-    k1_sweep<TX>(p);
     if (L.kind == K1_VTI_VEL) {
         static bool attr = false;
         Maps<6> mp;
         for (int i = 0; i < 6; ++i) mp.m[i] = L.maps[i];
-        return k1_launch(vti_vel<TX, S>, 32 * TX + 32, VtiVelL<TX, S>::TOTAL, p.sw.W, L.grid, st, attr,
+        const int grid = k1_sweep<TX>(p, vti_vel<TX, S>, 32 * TX + 32, VtiVelL<TX, S>::TOTAL, L.grid);
+        return k1_launch(vti_vel<TX, S>, 32 * TX + 32, VtiVelL<TX, S>::TOTAL, p.sw.W, grid, st, attr,
                          mp, (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
     static bool attr = false;
     Maps<9> mp;
     for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
-    return k1_launch(vti_stress<TX, S>, 32 * TX + 32, VtiStrL<TX, S>::TOTAL, p.sw.W, L.grid, st, attr,
+    const int grid = k1_sweep<TX>(p, vti_stress<TX, S>, 32 * TX + 32, VtiStrL<TX, S>::TOTAL, L.grid);
+    return k1_launch(vti_stress<TX, S>, 32 * TX + 32, VtiStrL<TX, S>::TOTAL, p.sw.W, grid, st, attr,
                      mp, (S *)L.out0, (S *)L.out1, p);
 }
 

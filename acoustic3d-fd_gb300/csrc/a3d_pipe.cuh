@@ -40,9 +40,13 @@ struct Seg {
 template <int TX>
 __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long w1, long long &wend) {
     Seg s;
-    s.tile = (int)(w / sw.NY);
-    s.ya = sw.y_begin + (int)(w % sw.NY);
-    wend = (long long)(s.tile + 1) * sw.NY;
+    const long long full = (long long)sw.ntz * sw.ntx * sw.Yc;  // units of a full chunk
+    const int c = (int)(w / full);
+    const long long r = w - c * full;
+    const int len = min(sw.Yc, sw.NY - c * sw.Yc);
+    s.tile = (int)(r / len);
+    s.ya = sw.y_begin + c * sw.Yc + (int)(r % len);
+    wend = c * full + (long long)(s.tile + 1) * len;
     if (wend > w1) wend = w1;
     s.yb = s.ya + (int)(wend - w);
     s.z0 = MM + 32 * (s.tile % sw.ntz);
@@ -58,27 +62,26 @@ __device__ __forceinline__ void pipe_produce(const Sweep &sw, long long w0, long
                                              size_t strideA, uint32_t bytesA, unsigned char *ringB,
                                              size_t strideB, uint32_t bytesB, int *err,
                                              IssueA issueA, IssueB issueB) {
+    static_assert((KA & (KA - 1)) == 0 && (KB & (KB - 1)) == 0, "ring sizes are powers of two");
     volatile int *ab = b.abort_ptr();
-    long long ja = 0, jb = 0;
+    uint32_t ja = 0, jb = 0;
     bool ok = true;
     for (long long w = w0; w < w1 && ok;) {
         long long wend;
         const Seg s = make_seg<TX>(sw, w, w1, wend);
         for (int q = s.ya - MM; q < s.yb + MM; ++q) {
-            const int sa = (int)(ja % KA);
+            const uint32_t sa = ja % KA;
             if (ja >= KA)
-                ok = mbar_wait(&b.emptyA[sa], (uint32_t)(((ja / KA) - 1) & 1), err,
-                               KERR_EMPTY_TIMEOUT, ab);
+                ok = mbar_wait(&b.emptyA[sa], ((ja / KA) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab);
             if (!ok) break;
             mbar_arrive_expect_tx(&b.fullA[sa], bytesA);
             issueA(ringA + sa * strideA, &b.fullA[sa], s, q);
             ++ja;
             const int o = q - MM;
             if (o >= s.ya) {
-                const int sb = (int)(jb % KB);
+                const uint32_t sb = jb % KB;
                 if (jb >= KB)
-                    ok = mbar_wait(&b.emptyB[sb], (uint32_t)(((jb / KB) - 1) & 1), err,
-                                   KERR_EMPTY_TIMEOUT, ab);
+                    ok = mbar_wait(&b.emptyB[sb], ((jb / KB) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab);
                 if (!ok) break;
                 mbar_arrive_expect_tx(&b.fullB[sb], bytesB);
                 issueB(ringB + sb * strideB, &b.fullB[sb], s, o);
@@ -88,12 +91,10 @@ __device__ __forceinline__ void pipe_produce(const Sweep &sw, long long w0, long
         w = wend;
     }
     // drain: every issued copy must land before the CTA's shared memory goes away
-    for (long long j = (ja > KA ? ja - KA : 0); j < ja; ++j)
-        if (!mbar_wait(&b.fullA[j % KA], (uint32_t)((j / KA) & 1), err, KERR_DRAIN_TIMEOUT, ab))
-            break;
-    for (long long j = (jb > KB ? jb - KB : 0); j < jb; ++j)
-        if (!mbar_wait(&b.fullB[j % KB], (uint32_t)((j / KB) & 1), err, KERR_DRAIN_TIMEOUT, ab))
-            break;
+    for (uint32_t j = (ja > KA ? ja - KA : 0); j < ja; ++j)
+        if (!mbar_wait(&b.fullA[j % KA], (j / KA) & 1, err, KERR_DRAIN_TIMEOUT, ab)) break;
+    for (uint32_t j = (jb > KB ? jb - KB : 0); j < jb; ++j)
+        if (!mbar_wait(&b.fullB[j % KB], (j / KB) & 1, err, KERR_DRAIN_TIMEOUT, ab)) break;
 }
 
 // Consumers: all consumer threads.  onSeg(seg) at a segment start; onLoad(stageA, seg, q)
@@ -105,22 +106,19 @@ __device__ __forceinline__ bool pipe_consume(const Sweep &sw, long long w0, long
                                              size_t strideA, unsigned char *ringB, size_t strideB,
                                              int *err, OnSeg onSeg, OnLoad onLoad, OnOut onOut) {
     volatile int *ab = b.abort_ptr();
-    long long ja = 0, jb = 0;
+    uint32_t ja = 0, jb = 0;
     for (long long w = w0; w < w1;) {
         long long wend;
         const Seg s = make_seg<TX>(sw, w, w1, wend);
         onSeg(s);
         for (int q = s.ya - MM; q < s.yb + MM; ++q) {
-            const int sa = (int)(ja % KA);
-            if (!mbar_wait(&b.fullA[sa], (uint32_t)((ja / KA) & 1), err, KERR_FULL_TIMEOUT, ab))
-                return false;
+            const uint32_t sa = ja % KA;
+            if (!mbar_wait(&b.fullA[sa], (ja / KA) & 1, err, KERR_FULL_TIMEOUT, ab)) return false;
             onLoad(ringA + sa * strideA, s, q);
             const int o = q - MM;
             if (o >= s.ya) {
-                const int sb = (int)(jb % KB);
-                if (!mbar_wait(&b.fullB[sb], (uint32_t)((jb / KB) & 1), err, KERR_FULL_TIMEOUT,
-                               ab))
-                    return false;
+                const uint32_t sb = jb % KB;
+                if (!mbar_wait(&b.fullB[sb], (jb / KB) & 1, err, KERR_FULL_TIMEOUT, ab)) return false;
                 onOut(ringA + ((ja - MM) % KA) * strideA, ringB + sb * strideB, s, o);
                 mbar_arrive(&b.emptyB[sb]);
                 ++jb;

@@ -11,6 +11,8 @@ namespace a3d {
 static const double PI_REF = 3.141592653;  // the reference's pi / PI macro (2O:14, ISO:28)
 
 void pad_model(const float *m, const Grid &g, float *out) {
+    for (size_t i = 0; i < g.elems(); ++i) out[i] = 0.0f;
+    out += Grid::zoff;
     for (int iy = 0; iy < g.nny; ++iy) {
         int cy = iy - g.pad;
         cy = cy < 0 ? 0 : (cy >= g.ny ? g.ny - 1 : cy);
@@ -24,7 +26,6 @@ void pad_model(const float *m, const Grid &g, float *out) {
                 cz = cz < 0 ? 0 : (cz >= g.nz ? g.nz - 1 : cz);
                 dst[iz] = src[cz];
             }
-            for (int iz = g.nnz; iz < g.ldz; ++iz) dst[iz] = 0.0f;
         }
     }
 }

@@ -8,23 +8,29 @@
 
 namespace a3d {
 
+// Device layout of a padded field: element (iz, ix, iy) at base + idx(iz, ix, iy),
+// base = allocation + zoff elements.  zoff = 28 puts the first updated cell of a
+// row (iz = 4) on a 128-byte boundary, and ldz (a multiple of 32 elements) keeps
+// every row so, which is what makes the kernels' 32-wide TMA boxes whole sectors.
 struct Grid {
+    static constexpr int zoff = 28;
     int nx = 0, ny = 0, nz = 0;  // model
     int pad = 0;                 // cells added on every face
     int nnx = 0, nny = 0, nnz = 0, ldz = 0;
     void set(int nx_, int ny_, int nz_, int pad_) {
         nx = nx_; ny = ny_; nz = nz_; pad = pad_;
         nnx = nx + 2 * pad; nny = ny + 2 * pad; nnz = nz + 2 * pad;
-        ldz = (nnz + 7) / 8 * 8;  // 16-byte rows for every storage type
+        ldz = (zoff + nnz + 31) / 32 * 32;
     }
-    size_t elems() const { return (size_t)ldz * nnx * nny; }
+    size_t elems() const { return (size_t)ldz * nnx * nny; }  // allocation, in elements
     size_t idx(int iz, int ix, int iy) const {
         return (size_t)iz + (size_t)ldz * ((size_t)ix + (size_t)nnx * iy);
     }
 };
 
-// Edge-replicated copy of a model (z fastest, x, y) into the padded device
-// layout (ldz rows); the reference's three one-axis copies compose to a clamp.
+// Edge-replicated copy of a model (z fastest, x, y) into a host image of a field
+// allocation (elems() floats; the field base sits zoff elements in); the
+// reference's three one-axis copies compose to a clamp.
 void pad_model(const float *m, const Grid &g, float *out);
 
 float ricker2o(int it, float dt, float fm);          // Toa_3dfd_cuda.cu:34-43
