@@ -77,6 +77,8 @@ def lib() -> ctypes.CDLL:
         L.a3d_engine_set_profiling.restype = ctypes.c_int
         L.a3d_engine_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]
         L.a3d_engine_kernel_times.restype = ctypes.c_int
+        L.a3d_engine_describe.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+        L.a3d_engine_describe.restype = ctypes.c_int
         L.a3d_last_error.argtypes = []
         L.a3d_last_error.restype = ctypes.c_char_p
         _lib = L
@@ -172,6 +174,12 @@ class Engine:
         n = (ctypes.c_longlong * 2)()
         _check(lib().a3d_engine_kernel_times(self.h, ms, n))
         return [ms[0], ms[1]], [n[0], n[1]]
+
+    def describe(self) -> dict:
+        import json
+        buf = ctypes.create_string_buffer(2048)
+        _check(lib().a3d_engine_describe(self.h, buf, len(buf)))
+        return json.loads(buf.value.decode())
 
     def record_device_ptr(self) -> int:
         return lib().a3d_engine_record_device(self.h)

@@ -35,10 +35,17 @@ void clear_error() { g_err.clear(); }
     } while (0)
 
 static int g_sms = 0;
-int plan_sweep(Sweep &sw, int occ) {
+int plan_sweep(Sweep &sw, int occ, int mode) {
     const long long slots = (long long)(g_sms > 0 ? g_sms : 148) * (occ > 0 ? occ : 1);
     const long long ntiles = (long long)sw.ntz * sw.ntx;
     sw.W = ntiles * sw.NY;
+    if (mode == 1) {  // fill: one full wave, chunk length from the nearest chunk count
+        long long C = (slots + ntiles / 2) / ntiles;
+        const long long cmax = sw.NY / 16 > 1 ? sw.NY / 16 : 1;
+        C = C < 1 ? 1 : (C > cmax ? cmax : C);
+        sw.Yc = (int)((sw.NY + C - 1) / C);
+        return (int)(slots < sw.W / 16 ? slots : (sw.W / 16 > 0 ? sw.W / 16 : 1));
+    }
     if (ntiles <= slots) {
         long long C = slots / ntiles;
         const long long cmax = sw.NY / 16 > 1 ? sw.NY / 16 : 1;
@@ -183,11 +190,15 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
         for (int it = 0; it < c.nt; ++it) e->w2o[it] = ricker2o(it, c.dt, c.fm);
         const bool f64 = e->fp64;
         void *buf[2] = {e->X, e->Y};
-        for (int b = 0; b < 2; ++b) {
-            if ((rc = make_map(&e->m2o_cur[b], buf[b], f64, g, 40, e->tx + 8))) return rc;
-            if ((rc = make_map(&e->m2o_prev[b], buf[b], f64, g, 32, e->tx))) return rc;
+        for (int t = 0; t < 2; ++t) {
+            const int tx = t ? 16 : 8;
+            for (int b = 0; b < 2; ++b) {
+                if ((rc = make_map(&e->m2o_cur[t][b], buf[b], f64, g, 40, tx + 8))) return rc;
+                if ((rc = make_map(&e->m2o_prev[t][b], buf[b], f64, g, 32, tx))) return rc;
+            }
+            if ((rc = make_map(&e->m2o_vv[t], e->vv, false, g, 32, tx))) return rc;
         }
-        return make_map(&e->m2o_vv, e->vv, false, g, 32, e->tx);
+        return A3D_OK;
     }
 
     // 1st-order engines
@@ -263,9 +274,11 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
             e->amp1[it] = pfac * src;
         }
     }
-    // tensor maps
+    // tensor maps for both tile widths
     const bool f64 = e->fp64;
-    const int tx = e->tx;
+    for (int t = 0; t < 2; ++t) {
+    const int tx = t ? 16 : 8;
+    CUtensorMap *mvel = e->mvel[t], *mstr = e->mstr[t];
     int b0, b1;
     auto mk = [&](CUtensorMap *m, const void *p, bool isfield, int box) {
         box_dims(box, tx, b0, b1);
@@ -273,44 +286,45 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     };
     if (c.physics == A3D_ISO) {
         e->nvel = 5;
-        if ((rc = mk(&e->mvel[0], e->P, true, BOX_H)) || (rc = mk(&e->mvel[1], e->u, true, BOX_CORE)) ||
-            (rc = mk(&e->mvel[2], e->v, true, BOX_CORE)) || (rc = mk(&e->mvel[3], e->w, true, BOX_CORE)) ||
-            (rc = mk(&e->mvel[4], e->rho, false, BOX_CORE)))
+        if ((rc = mk(&mvel[0], e->P, true, BOX_H)) || (rc = mk(&mvel[1], e->u, true, BOX_CORE)) ||
+            (rc = mk(&mvel[2], e->v, true, BOX_CORE)) || (rc = mk(&mvel[3], e->w, true, BOX_CORE)) ||
+            (rc = mk(&mvel[4], e->rho, false, BOX_CORE)))
             return rc;
         e->nstr = 6;
-        if ((rc = mk(&e->mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&e->mstr[1], e->u, true, BOX_HX)) ||
-            (rc = mk(&e->mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&e->mstr[3], e->P, true, BOX_CORE)) ||
-            (rc = mk(&e->mstr[4], e->rho, false, BOX_CORE)) || (rc = mk(&e->mstr[5], e->vp, false, BOX_CORE)))
+        if ((rc = mk(&mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&mstr[1], e->u, true, BOX_HX)) ||
+            (rc = mk(&mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&mstr[3], e->P, true, BOX_CORE)) ||
+            (rc = mk(&mstr[4], e->rho, false, BOX_CORE)) || (rc = mk(&mstr[5], e->vp, false, BOX_CORE)))
             return rc;
     } else if (c.physics == A3D_VTI) {
         e->nvel = 6;
-        if ((rc = mk(&e->mvel[0], e->P, true, BOX_HX)) || (rc = mk(&e->mvel[1], e->Q, true, BOX_HZ)) ||
-            (rc = mk(&e->mvel[2], e->u, true, BOX_CORE)) || (rc = mk(&e->mvel[3], e->v, true, BOX_CORE)) ||
-            (rc = mk(&e->mvel[4], e->w, true, BOX_CORE)) || (rc = mk(&e->mvel[5], e->rho, false, BOX_CORE)))
+        if ((rc = mk(&mvel[0], e->P, true, BOX_HX)) || (rc = mk(&mvel[1], e->Q, true, BOX_HZ)) ||
+            (rc = mk(&mvel[2], e->u, true, BOX_CORE)) || (rc = mk(&mvel[3], e->v, true, BOX_CORE)) ||
+            (rc = mk(&mvel[4], e->w, true, BOX_CORE)) || (rc = mk(&mvel[5], e->rho, false, BOX_CORE)))
             return rc;
         e->nstr = 9;
-        if ((rc = mk(&e->mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&e->mstr[1], e->u, true, BOX_HX)) ||
-            (rc = mk(&e->mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&e->mstr[3], e->P, true, BOX_CORE)) ||
-            (rc = mk(&e->mstr[4], e->Q, true, BOX_CORE)) || (rc = mk(&e->mstr[5], e->rho, false, BOX_CORE)) ||
-            (rc = mk(&e->mstr[6], e->vp, false, BOX_CORE)) || (rc = mk(&e->mstr[7], e->eps, false, BOX_CORE)) ||
-            (rc = mk(&e->mstr[8], e->del, false, BOX_CORE)))
+        if ((rc = mk(&mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&mstr[1], e->u, true, BOX_HX)) ||
+            (rc = mk(&mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&mstr[3], e->P, true, BOX_CORE)) ||
+            (rc = mk(&mstr[4], e->Q, true, BOX_CORE)) || (rc = mk(&mstr[5], e->rho, false, BOX_CORE)) ||
+            (rc = mk(&mstr[6], e->vp, false, BOX_CORE)) || (rc = mk(&mstr[7], e->eps, false, BOX_CORE)) ||
+            (rc = mk(&mstr[8], e->del, false, BOX_CORE)))
             return rc;
     } else {
         e->nvel = 9;
-        if ((rc = mk(&e->mvel[0], e->P, true, BOX_H)) || (rc = mk(&e->mvel[1], e->Q, true, BOX_H)) ||
-            (rc = mk(&e->mvel[2], e->u, true, BOX_CORE)) || (rc = mk(&e->mvel[3], e->v, true, BOX_CORE)) ||
-            (rc = mk(&e->mvel[4], e->w, true, BOX_CORE)) || (rc = mk(&e->mvel[5], e->tct, false, BOX_CORE)) ||
-            (rc = mk(&e->mvel[6], e->tst, false, BOX_CORE)) || (rc = mk(&e->mvel[7], e->tcp, false, BOX_CORE)) ||
-            (rc = mk(&e->mvel[8], e->tsp, false, BOX_CORE)))
+        if ((rc = mk(&mvel[0], e->P, true, BOX_H)) || (rc = mk(&mvel[1], e->Q, true, BOX_H)) ||
+            (rc = mk(&mvel[2], e->u, true, BOX_CORE)) || (rc = mk(&mvel[3], e->v, true, BOX_CORE)) ||
+            (rc = mk(&mvel[4], e->w, true, BOX_CORE)) || (rc = mk(&mvel[5], e->tct, false, BOX_CORE)) ||
+            (rc = mk(&mvel[6], e->tst, false, BOX_CORE)) || (rc = mk(&mvel[7], e->tcp, false, BOX_CORE)) ||
+            (rc = mk(&mvel[8], e->tsp, false, BOX_CORE)))
             return rc;
         e->nstr = 12;
-        if ((rc = mk(&e->mstr[0], e->u, true, BOX_H)) || (rc = mk(&e->mstr[1], e->v, true, BOX_H)) ||
-            (rc = mk(&e->mstr[2], e->w, true, BOX_H)) || (rc = mk(&e->mstr[3], e->P, true, BOX_CORE)) ||
-            (rc = mk(&e->mstr[4], e->Q, true, BOX_CORE)) || (rc = mk(&e->mstr[5], e->vp, false, BOX_CORE)) ||
-            (rc = mk(&e->mstr[6], e->eps, false, BOX_CORE)) || (rc = mk(&e->mstr[7], e->del, false, BOX_CORE)) ||
-            (rc = mk(&e->mstr[8], e->tct, false, BOX_CORE)) || (rc = mk(&e->mstr[9], e->tst, false, BOX_CORE)) ||
-            (rc = mk(&e->mstr[10], e->tcp, false, BOX_CORE)) || (rc = mk(&e->mstr[11], e->tsp, false, BOX_CORE)))
+        if ((rc = mk(&mstr[0], e->u, true, BOX_H)) || (rc = mk(&mstr[1], e->v, true, BOX_H)) ||
+            (rc = mk(&mstr[2], e->w, true, BOX_H)) || (rc = mk(&mstr[3], e->P, true, BOX_CORE)) ||
+            (rc = mk(&mstr[4], e->Q, true, BOX_CORE)) || (rc = mk(&mstr[5], e->vp, false, BOX_CORE)) ||
+            (rc = mk(&mstr[6], e->eps, false, BOX_CORE)) || (rc = mk(&mstr[7], e->del, false, BOX_CORE)) ||
+            (rc = mk(&mstr[8], e->tct, false, BOX_CORE)) || (rc = mk(&mstr[9], e->tst, false, BOX_CORE)) ||
+            (rc = mk(&mstr[10], e->tcp, false, BOX_CORE)) || (rc = mk(&mstr[11], e->tsp, false, BOX_CORE)))
             return rc;
+    }
     }
     return A3D_OK;
 }
@@ -335,12 +349,99 @@ static int check_kernel_error(a3d_engine *e) {
     return A3D_OK;
 }
 
+// Autotuner: times every candidate launch configuration (tile width, ring depth,
+// sweep plan) of each kernel kind on this engine's own grid — 1 untimed and 3
+// timed launches each, CUDA events on the engine stream — and keeps the fastest.
+// Candidates that do not fit (shared memory) are skipped.  The wavefields hold
+// garbage afterwards; run() clears them before every shot.
+int a3d_engine::autotune() {
+    const a3d_config &c = cfg;
+    std::vector<Tune> cand;
+    const int fixed_tx = c.tile_x == 8 || c.tile_x == 16 ? c.tile_x : 0;
+    if (c.tile_x < 0 || fp64) {  // fixed defaults (and the FP64 run): 32x8, shallow rings, both plans
+        for (int m = 0; m < 2; ++m) cand.push_back(Tune{8, false, m});
+    } else {
+        for (int tx : {8, 16})
+            for (int d = 0; d < 2; ++d)
+                for (int m = 0; m < 2; ++m)
+                    if (!fixed_tx || tx == fixed_tx) cand.push_back(Tune{tx, d != 0, m});
+    }
+    const int kinds = c.physics == A3D_2ORDER ? 1 : 2;
+    cudaEvent_t t0, t1;
+    CUDA_TRY(cudaEventCreate(&t0));
+    CUDA_TRY(cudaEventCreate(&t1));
+    for (int k = 0; k < kinds; ++k) {
+        float best = 1e30f;
+        for (const Tune &tc : cand) {
+            const int ti = tc.tx == 16 ? 1 : 0;
+            auto launch_once = [&]() -> cudaError_t {
+                if (c.physics == A3D_2ORDER) {
+                    K2OLaunch L{};
+                    L.tx = tc.tx; L.deep = tc.deep; L.mode = tc.mode; L.fp64 = fp64;
+                    L.tm_cur = m2o_cur[ti][0]; L.tm_prev = m2o_prev[ti][1]; L.tm_vv = m2o_vv[ti];
+                    L.ybuf = Y;
+                    K2OParams &p = L.p;
+                    p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
+                    p.nx = c.nx; p.ny = c.ny; p.gz = -1;
+                    p.fz = fz; p.fx = fx; p.fy = fy;
+                    p.dz2 = p.dx2 = p.dy2 = 1.0f;
+                    p.s_x = p.s_y = p.s_z = -100;
+                    p.rec = rec; p.nt = c.nt; p.err = d_err;
+                    return launch_k2o(L, st);
+                }
+                K1Launch L{};
+                K1Params &p = L.p;
+                p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
+                p.nx = c.nx; p.ny = c.ny; p.npml = npml;
+                p.dtx = p.dty = p.dtz = 0.0f;
+                const float *q = pml;
+                p.cx1 = q; p.cx2 = q + g.nnx; p.ax1 = q + 2 * g.nnx; p.ax2 = q + 3 * g.nnx; q += 4 * g.nnx;
+                p.cy1 = q; p.cy2 = q + g.nny; p.ay1 = q + 2 * g.nny; p.ay2 = q + 3 * g.nny; q += 4 * g.nny;
+                p.cz1 = q; p.cz2 = q + g.nnz; p.az1 = q + 2 * g.nnz; p.az2 = q + 3 * g.nnz;
+                p.s_x = p.s_y = p.s_z = -100;
+                p.taper = taper;
+                p.px = px; p.py = py; p.pz = pz; p.qx = qx; p.qy = qy; p.qz = qz;
+                p.rec = rec; p.nt = c.nt; p.err = d_err;
+                const int kv = c.physics == A3D_ISO ? K1_ISO_VEL : (c.physics == A3D_VTI ? K1_VTI_VEL : K1_TTI_VEL);
+                L.kind = kv + k;
+                L.maps = k == 0 ? mvel[ti] : mstr[ti];
+                L.nmaps = k == 0 ? nvel : nstr;
+                L.out0 = k == 0 ? u : P; L.out1 = k == 0 ? v : Q; L.out2 = w;
+                L.tx = tc.tx; L.deep = tc.deep; L.mode = tc.mode; L.fp64 = fp64;
+                auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
+                return launch(L, st);
+            };
+            if (launch_once() != cudaSuccess) { cudaGetLastError(); continue; }
+            CUDA_TRY(cudaEventRecord(t0, st));
+            bool ok = true;
+            for (int r = 0; r < 3 && ok; ++r) ok = launch_once() == cudaSuccess;
+            CUDA_TRY(cudaEventRecord(t1, st));
+            CUDA_TRY(cudaEventSynchronize(t1));
+            if (!ok) { cudaGetLastError(); continue; }
+            float f = 0;
+            CUDA_TRY(cudaEventElapsedTime(&f, t0, t1));
+            if (f < best) {
+                best = f;
+                tune[k] = tc;
+                tune[k].ms = f / 3;
+            }
+        }
+        if (best >= 1e30f) return fail(A3D_E_CUDA, "no launch configuration of kernel kind %d runs", k);
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    tuned = true;
+    return check_kernel_error(this);
+}
+
 int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, double *ms) {
     const a3d_config &c = cfg;
     if (s.sx < 0 || s.sx >= c.nx || s.sy < 0 || s.sy >= c.ny || s.sz < 0 || s.sz >= c.nz)
         return fail(A3D_E_ARG, "shot (%d,%d,%d) outside the %dx%dx%d model", s.sx, s.sy, s.sz, c.nx, c.ny, c.nz);
     if (!rec_dev) rec_dev = rec;
     CUDA_TRY(cudaSetDevice(device));
+    int rc;
+    if (!tuned && (rc = autotune())) return rc;
     CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
     const size_t fb = g.elems() * esz;
     // direct-wave mute thresholds for this shot
@@ -365,7 +466,6 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         CUDA_TRY(cudaStreamSynchronize(st));
         return hook->take ? hook->take(it, snap_host.data()) : A3D_OK;
     };
-    int rc;
     if (c.physics == A3D_2ORDER) {
         CUDA_TRY(cudaMemsetAsync(field_alloc(X, esz), 0, fb, st));
         CUDA_TRY(cudaMemsetAsync(field_alloc(Y, esz), 0, fb, st));
@@ -381,10 +481,13 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
             CUDA_TRY(cudaMemcpyAsync((float *)X + si, d, sizeof d, cudaMemcpyHostToDevice, st));
         }
         K2OLaunch L{};
-        L.tx = tx;
+        const int ti = tune[0].tx == 16 ? 1 : 0;
+        L.tx = tune[0].tx;
+        L.deep = tune[0].deep;
+        L.mode = tune[0].mode;
         L.fp64 = fp64;
         L.grid = 0;
-        L.tm_vv = m2o_vv;
+        L.tm_vv = m2o_vv[ti];
         K2OParams &p = L.p;
         p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
         p.nx = c.nx; p.ny = c.ny;
@@ -403,8 +506,8 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         if ((rc = prepare_profiling(this, 2))) return rc;
         CUDA_TRY(cudaEventRecord(ev0, st));
         for (int it = 0; it < c.nt; ++it) {
-            L.tm_cur = m2o_cur[cur];
-            L.tm_prev = m2o_prev[1 - cur];
+            L.tm_cur = m2o_cur[ti][cur];
+            L.tm_prev = m2o_prev[ti][1 - cur];
             L.ybuf = buf[1 - cur];
             p.w_next = it + 1 < c.nt ? w2o[it + 1] : 0.0f;
             p.it = it;
@@ -438,10 +541,13 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         p.err = d_err;
         const int kv = c.physics == A3D_ISO ? K1_ISO_VEL : (c.physics == A3D_VTI ? K1_VTI_VEL : K1_TTI_VEL);
         Lv.kind = kv; Ls.kind = kv + 1;
-        Lv.maps = mvel; Lv.nmaps = nvel; Ls.maps = mstr; Ls.nmaps = nstr;
+        Lv.maps = mvel[tune[0].tx == 16 ? 1 : 0]; Lv.nmaps = nvel;
+        Ls.maps = mstr[tune[1].tx == 16 ? 1 : 0]; Ls.nmaps = nstr;
         Lv.out0 = u; Lv.out1 = v; Lv.out2 = w;
         Ls.out0 = P; Ls.out1 = Q;
-        Lv.tx = Ls.tx = tx; Lv.fp64 = Ls.fp64 = fp64; Lv.grid = Ls.grid = 0;
+        Lv.tx = tune[0].tx; Lv.deep = tune[0].deep; Lv.mode = tune[0].mode;
+        Ls.tx = tune[1].tx; Ls.deep = tune[1].deep; Ls.mode = tune[1].mode;
+        Lv.fp64 = Ls.fp64 = fp64; Lv.grid = Ls.grid = 0;
         auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
         if ((rc = prepare_profiling(this, 3))) return rc;
         CUDA_TRY(cudaEventRecord(ev0, st));
@@ -520,8 +626,7 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
     e->device = device;
     e->fp64 = cfg->storage == A3D_FP64;
     e->esz = e->fp64 ? 8 : 4;
-    e->tx = cfg->tile_x == 4 || cfg->tile_x == 16 ? cfg->tile_x : 8;
-    if (e->fp64 && e->tx == 16) e->tx = 8;
+    e->tx = 8;
     if (ph == A3D_2ORDER) {
         e->npml = cfg->npml > 0 ? cfg->npml : 50;  // npd, 2O:19
         if (e->cfg.rec_z < 0) e->cfg.rec_z = 1;    // 2O:159 records at model depth 1
@@ -612,6 +717,22 @@ extern "C" int a3d_engine_kernel_times(const a3d_engine *e, double *ms, long lon
         if (ms) ms[k] = e->kms[k];
         if (launches) launches[k] = e->klaunch[k];
     }
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_describe(a3d_engine *e, char *buf, size_t n) {
+    if (!e || !buf || n == 0) return fail(A3D_E_ARG, "null engine or buffer");
+    if (!e->tuned) {
+        CUDA_TRY(cudaSetDevice(e->device));
+        int rc = e->autotune();
+        if (rc) return rc;
+    }
+    snprintf(buf, n,
+             "{\"grid\": [%d, %d, %d], \"ldz\": %d, \"pad\": %d, \"device_bytes\": %zu, "
+             "\"kernels\": [{\"tile_x\": %d, \"deep\": %d, \"plan\": %d, \"ms\": %.4f}, "
+             "{\"tile_x\": %d, \"deep\": %d, \"plan\": %d, \"ms\": %.4f}]}",
+             e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, e->tune[0].tx, (int)e->tune[0].deep,
+             e->tune[0].mode, e->tune[0].ms, e->tune[1].tx, (int)e->tune[1].deep, e->tune[1].mode, e->tune[1].ms);
     return A3D_OK;
 }
 

@@ -60,10 +60,17 @@ struct a3d_engine {
     float *snap_dev = nullptr;
     std::vector<float> snap_host;
 
-    // tensor maps
-    CUtensorMap m2o_cur[2], m2o_prev[2], m2o_vv;
-    CUtensorMap mvel[9], mstr[12];
+    // tensor maps for the two tile widths (index 0: 32x8 tiles, 1: 32x16)
+    CUtensorMap m2o_cur[2][2], m2o_prev[2][2], m2o_vv[2];  // [tile][buffer]
+    CUtensorMap mvel[2][9], mstr[2][12];
     int nvel = 0, nstr = 0;
+
+    // launch configuration per kernel kind ([0] velocity / 2nd-order step, [1] stress),
+    // chosen by the autotuner on the first run unless fixed by the config
+    struct Tune { int tx = 8; bool deep = false; int mode = 0; float ms = 0; };
+    Tune tune[2];
+    bool tuned = false;
+    int autotune();
 
     // optional per-kernel timing: events around every launch of each kernel kind
     bool profiling = false;

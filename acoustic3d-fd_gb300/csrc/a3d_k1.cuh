@@ -39,6 +39,8 @@ struct K1Launch {
     K1Params p;
     int tx, grid;
     bool fp64;
+    bool deep;  // deep TMA rings
+    int mode;   // sweep plan (plan_sweep)
 };
 
 cudaError_t launch_k1(const K1Launch &L, cudaStream_t st);

@@ -54,7 +54,7 @@ static cudaError_t k1_launch(Kern kern, int nthreads, size_t smem, long long W, 
 
 // sweep of the updated region [4, nn-4)^3 in 32 x TX tiles; returns gridDim.x
 template <int TX, class Kern>
-static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid) {
+static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid, int mode) {
     p.sw.ntz = (p.nnz - 2 * MM + 31) / 32;
     p.sw.ntx = (p.nnx - 2 * MM + TX - 1) / TX;
     p.sw.y_begin = MM;
@@ -62,7 +62,7 @@ static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid)
     int occ = 0;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nthreads, smem);
-    const int g = plan_sweep(p.sw, occ);
+    const int g = plan_sweep(p.sw, occ, mode);
     return grid > 0 ? grid : g;
 }
 

@@ -22,10 +22,10 @@
 
 namespace a3d {
 
-template <int TX, class S>
+template <int TX, class S, int D>
 struct K2OSmem {
-    static constexpr int KA = 8;  // halo'd current-level stages (5 live + 3 in flight)
-    static constexpr int KB = 4;  // prev/vv stages
+    static constexpr int KA = Depth<D>::KA;  // halo'd current-level stages (4 live + rest in flight)
+    static constexpr int KB = Depth<D>::KB;  // prev/vv stages
     static constexpr int AW = 40, AH = TX + 8;  // A tile: [AH][AW]
     static constexpr int A_ELEMS = AW * AH;
     static constexpr int B_ELEMS = 32 * TX;
@@ -38,12 +38,12 @@ struct K2OSmem {
     static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBars<KA, KB>);
 };
 
-template <int TX, class S>
+template <int TX, class S, int D>
 __global__ void __launch_bounds__(32 * TX + 32)
     k2o_step(const __grid_constant__ CUtensorMap tm_cur, const __grid_constant__ CUtensorMap tm_prev,
              const __grid_constant__ CUtensorMap tm_vv, S *__restrict__ ybuf,
              const __grid_constant__ K2OParams p) {
-    using L = K2OSmem<TX, S>;
+    using L = K2OSmem<TX, S, D>;
     using T = typename Arith<S>::T;
     constexpr int NC = 32 * TX;  // consumer threads
     extern __shared__ __align__(128) unsigned char smem[];
@@ -149,10 +149,10 @@ __global__ void __launch_bounds__(32 * TX + 32)
 // ---------------------------------------------------------------------------
 // host launcher
 
-template <int TX, class S>
+template <int TX, class S, int D>
 static cudaError_t launch_k2o_t(const K2OLaunch &L, cudaStream_t st) {
-    using SM = K2OSmem<TX, S>;
-    auto kern = k2o_step<TX, S>;
+    using SM = K2OSmem<TX, S, D>;
+    auto kern = k2o_step<TX, S, D>;
     static bool attr_done = false;
     if (!attr_done) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -167,7 +167,7 @@ static cudaError_t launch_k2o_t(const K2OLaunch &L, cudaStream_t st) {
     p.sw.NY = p.nny - 2 * MM;
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * TX + 32, SM::TOTAL);
-    int grid = plan_sweep(p.sw, occ);
+    int grid = plan_sweep(p.sw, occ, L.mode);
     if (L.grid > 0) grid = L.grid;
     kern<<<grid, 32 * TX + 32, SM::TOTAL, st>>>(L.tm_cur, L.tm_prev, L.tm_vv,
                                                 reinterpret_cast<S *>(L.ybuf), p);
@@ -175,23 +175,14 @@ static cudaError_t launch_k2o_t(const K2OLaunch &L, cudaStream_t st) {
 }
 
 cudaError_t launch_k2o(const K2OLaunch &L, cudaStream_t st) {
-    if (L.fp64) {
-        switch (L.tx) {
-            case 4: return launch_k2o_t<4, double>(L, st);
-            default: return launch_k2o_t<8, double>(L, st);
-        }
-    }
-    switch (L.tx) {
-        case 4: return launch_k2o_t<4, float>(L, st);
-        case 16: return launch_k2o_t<16, float>(L, st);
-        default: return launch_k2o_t<8, float>(L, st);
-    }
+    if (L.fp64) return launch_k2o_t<8, double, 0>(L, st);
+    if (L.tx == 16) return L.deep ? launch_k2o_t<16, float, 1>(L, st) : launch_k2o_t<16, float, 0>(L, st);
+    return L.deep ? launch_k2o_t<8, float, 1>(L, st) : launch_k2o_t<8, float, 0>(L, st);
 }
 
 size_t k2o_smem_bytes(int tx, bool fp64) {
-    if (fp64) return tx == 4 ? K2OSmem<4, double>::TOTAL : K2OSmem<8, double>::TOTAL;
-    return tx == 4 ? K2OSmem<4, float>::TOTAL
-                   : (tx == 16 ? K2OSmem<16, float>::TOTAL : K2OSmem<8, float>::TOTAL);
+    if (fp64) return K2OSmem<8, double, 0>::TOTAL;
+    return tx == 16 ? K2OSmem<16, float, 0>::TOTAL : K2OSmem<8, float, 0>::TOTAL;
 }
 
 }  // namespace a3d

@@ -53,18 +53,22 @@ struct K2OLaunch {
     CUtensorMap tm_cur, tm_prev, tm_vv;
     void *ybuf;  // previous-level buffer, overwritten with the next level
     K2OParams p;
-    int tx;      // tile width along x (4, 8, 16)
-    int grid;    // CTAs (0: one wave at full occupancy)
+    int tx;      // tile width along x (8, 16)
+    int grid;    // CTAs (0: planned from the occupancy)
     bool fp64;
+    bool deep;   // deep TMA rings (16 + 8 stages) instead of 8 + 4
+    int mode;    // sweep plan (plan_sweep)
 };
 
 cudaError_t launch_k2o(const K2OLaunch &L, cudaStream_t st);
 size_t k2o_smem_bytes(int tx, bool fp64);
 
 // Pick gridDim.x and the y-chunk length of a sweep (ntz, ntx, NY already set)
-// for occ_per_sm resident CTAs per SM: if every tile fits in one wave, one CTA
-// per (tile, chunk) with as many chunks as the wave holds (each >= 16 planes);
-// otherwise one wave of CTAs over whole-y segments.  Fills sw.Yc and sw.W.
-int plan_sweep(Sweep &sw, int occ_per_sm);
+// for occ_per_sm resident CTAs per SM.  Mode 0 (lockstep): if every tile fits
+// in one wave, one CTA per (tile, chunk) with as many chunks as the wave holds
+// (each >= 16 planes), otherwise one wave over whole-y segments.  Mode 1 (fill):
+// one full wave of CTAs, the chunk count rounded to the nearest fit.
+// Fills sw.Yc and sw.W.
+int plan_sweep(Sweep &sw, int occ_per_sm, int mode);
 
 }  // namespace a3d

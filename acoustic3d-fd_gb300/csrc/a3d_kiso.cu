@@ -14,9 +14,9 @@ namespace a3d {
 
 // ===========================================================================
 // iso_vel: maps {P (box H), u, v, w (core), rho (core, float)}
-template <int TX, class S>
+template <int TX, class S, int D>
 struct IsoVelL {
-    static constexpr int KA = 8, KB = 4;
+    static constexpr int KA = Depth<D>::KA, KB = Depth<D>::KB;
     static constexpr int AW = 40, AH = TX + 8;
     static constexpr uint32_t A_BYTES = AW * AH * sizeof(S);
     static constexpr uint32_t C = 32 * TX;  // core elements
@@ -27,11 +27,11 @@ struct IsoVelL {
     static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBars<KA, KB>);
 };
 
-template <int TX, class S>
+template <int TX, class S, int D>
 __global__ void __launch_bounds__(32 * TX + 32)
     iso_vel(const __grid_constant__ Maps<5> mp, S *__restrict__ u, S *__restrict__ v,
             S *__restrict__ w, const __grid_constant__ K1Params p) {
-    using L = IsoVelL<TX, S>;
+    using L = IsoVelL<TX, S, D>;
     using T = typename Arith<S>::T;
     constexpr int NC = 32 * TX;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -125,9 +125,9 @@ __global__ void __launch_bounds__(32 * TX + 32)
 
 // ===========================================================================
 // iso_stress: maps {v (core), u (box HX), w (box HZ), P (core), rho, vp (core, float)}
-template <int TX, class S>
+template <int TX, class S, int D>
 struct IsoStrL {
-    static constexpr int KA = 8, KB = 4;
+    static constexpr int KA = Depth<D>::KA, KB = Depth<D>::KB;
     static constexpr uint32_t C = 32 * TX;
     static constexpr uint32_t UX = 32 * (TX + 8), WZ = 40 * TX;
     static constexpr uint32_t A_BYTES = C * sizeof(S);
@@ -138,11 +138,11 @@ struct IsoStrL {
     static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBars<KA, KB>);
 };
 
-template <int TX, class S>
+template <int TX, class S, int D>
 __global__ void __launch_bounds__(32 * TX + 32)
     iso_stress(const __grid_constant__ Maps<6> mp, S *__restrict__ P,
                const __grid_constant__ K1Params p) {
-    using L = IsoStrL<TX, S>;
+    using L = IsoStrL<TX, S, D>;
     using T = typename Arith<S>::T;
     constexpr int NC = 32 * TX;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -240,33 +240,30 @@ __global__ void __launch_bounds__(32 * TX + 32)
 }
 
 // ===========================================================================
-template <int TX, class S>
+template <int TX, class S, int D>
 static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
     if (L.kind == K1_ISO_VEL) {
         static bool attr = false;
         Maps<5> mp;
         for (int i = 0; i < 5; ++i) mp.m[i] = L.maps[i];
-        auto kern = iso_vel<TX, S>;
-        const int grid = k1_sweep<TX>(p, kern, 32 * TX + 32, IsoVelL<TX, S>::TOTAL, L.grid);
-        return k1_launch(kern, 32 * TX + 32, IsoVelL<TX, S>::TOTAL, p.sw.W, grid, st, attr, mp,
+        auto kern = iso_vel<TX, S, D>;
+        const int grid = k1_sweep<TX>(p, kern, 32 * TX + 32, IsoVelL<TX, S, D>::TOTAL, L.grid, L.mode);
+        return k1_launch(kern, 32 * TX + 32, IsoVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp,
                          (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
     static bool attr = false;
     Maps<6> mp;
     for (int i = 0; i < 6; ++i) mp.m[i] = L.maps[i];
-    auto kern = iso_stress<TX, S>;
-    const int grid = k1_sweep<TX>(p, kern, 32 * TX + 32, IsoStrL<TX, S>::TOTAL, L.grid);
-    return k1_launch(kern, 32 * TX + 32, IsoStrL<TX, S>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, p);
+    auto kern = iso_stress<TX, S, D>;
+    const int grid = k1_sweep<TX>(p, kern, 32 * TX + 32, IsoStrL<TX, S, D>::TOTAL, L.grid, L.mode);
+    return k1_launch(kern, 32 * TX + 32, IsoStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, p);
 }
 
 cudaError_t launch_iso(const K1Launch &L, cudaStream_t st) {
-    if (L.fp64) return L.tx == 4 ? launch_iso_t<4, double>(L, st) : launch_iso_t<8, double>(L, st);
-    switch (L.tx) {
-        case 4: return launch_iso_t<4, float>(L, st);
-        case 16: return launch_iso_t<16, float>(L, st);
-        default: return launch_iso_t<8, float>(L, st);
-    }
+    if (L.fp64) return launch_iso_t<8, double, 0>(L, st);
+    if (L.tx == 16) return L.deep ? launch_iso_t<16, float, 1>(L, st) : launch_iso_t<16, float, 0>(L, st);
+    return L.deep ? launch_iso_t<8, float, 1>(L, st) : launch_iso_t<8, float, 0>(L, st);
 }
 
 }  // namespace a3d

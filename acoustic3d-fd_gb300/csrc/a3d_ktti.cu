@@ -12,9 +12,9 @@ namespace a3d {
 
 // ===========================================================================
 // tti_vel: maps {P (H), Q (H), u, v, w (core), ct, st, cp, sp (core float)}
-template <int TX, class S>
+template <int TX, class S, int D>
 struct TtiVelL {
-    static constexpr int KA = 8, KB = 4;
+    static constexpr int KA = Depth<D>::KA, KB = Depth<D>::KB;
     static constexpr int AW = 40, AH = TX + 8;
     static constexpr uint32_t C = 32 * TX, H = AW * AH;
     static constexpr uint32_t A_BYTES = 2 * H * sizeof(S);
@@ -34,11 +34,11 @@ __device__ __forceinline__ void tti_rot(T ct, T st, T cp, T sp, T ax, T ay, T az
     zz = fma_t(ct, cz_, fma_t(st * cp, cx_, -((st * sp) * cy_)));
 }
 
-template <int TX, class S>
+template <int TX, class S, int D>
 __global__ void __launch_bounds__(32 * TX + 32)
     tti_vel(const __grid_constant__ Maps<9> mp, S *__restrict__ u, S *__restrict__ v,
             S *__restrict__ w, const __grid_constant__ K1Params p) {
-    using L = TtiVelL<TX, S>;
+    using L = TtiVelL<TX, S, D>;
     using T = typename Arith<S>::T;
     constexpr int NC = 32 * TX;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -131,9 +131,9 @@ __global__ void __launch_bounds__(32 * TX + 32)
 
 // ===========================================================================
 // tti_stress: maps {u, v, w (H), P, Q (core), vp, eps, del, ct, st, cp, sp (core float)}
-template <int TX, class S>
+template <int TX, class S, int D>
 struct TtiStrL {
-    static constexpr int KA = 8, KB = 4;
+    static constexpr int KA = Depth<D>::KA, KB = Depth<D>::KB;
     static constexpr int AW = 40, AH = TX + 8;
     static constexpr uint32_t C = 32 * TX, H = AW * AH;
     static constexpr uint32_t A_BYTES = 3 * H * sizeof(S);
@@ -154,11 +154,11 @@ __device__ __forceinline__ void sv_eedd_t(const K1Params &p, int ix, int iy, int
     dd = mul_df(del, t.x, t.y);
 }
 
-template <int TX, class S>
+template <int TX, class S, int D>
 __global__ void __launch_bounds__(32 * TX + 32)
     tti_stress(const __grid_constant__ Maps<12> mp, S *__restrict__ P, S *__restrict__ Q,
                const __grid_constant__ K1Params p) {
-    using L = TtiStrL<TX, S>;
+    using L = TtiStrL<TX, S, D>;
     using T = typename Arith<S>::T;
     constexpr int NC = 32 * TX;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -271,32 +271,29 @@ __global__ void __launch_bounds__(32 * TX + 32)
         });
 }
 
-template <int TX, class S>
+template <int TX, class S, int D>
 static cudaError_t launch_tti_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
     if (L.kind == K1_TTI_VEL) {
         static bool attr = false;
         Maps<9> mp;
         for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
-        const int grid = k1_sweep<TX>(p, tti_vel<TX, S>, 32 * TX + 32, TtiVelL<TX, S>::TOTAL, L.grid);
-        return k1_launch(tti_vel<TX, S>, 32 * TX + 32, TtiVelL<TX, S>::TOTAL, p.sw.W, grid, st, attr,
+        const int grid = k1_sweep<TX>(p, tti_vel<TX, S, D>, 32 * TX + 32, TtiVelL<TX, S, D>::TOTAL, L.grid, L.mode);
+        return k1_launch(tti_vel<TX, S, D>, 32 * TX + 32, TtiVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr,
                          mp, (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
     static bool attr = false;
     Maps<12> mp;
     for (int i = 0; i < 12; ++i) mp.m[i] = L.maps[i];
-    const int grid = k1_sweep<TX>(p, tti_stress<TX, S>, 32 * TX + 32, TtiStrL<TX, S>::TOTAL, L.grid);
-    return k1_launch(tti_stress<TX, S>, 32 * TX + 32, TtiStrL<TX, S>::TOTAL, p.sw.W, grid, st, attr,
+    const int grid = k1_sweep<TX>(p, tti_stress<TX, S, D>, 32 * TX + 32, TtiStrL<TX, S, D>::TOTAL, L.grid, L.mode);
+    return k1_launch(tti_stress<TX, S, D>, 32 * TX + 32, TtiStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr,
                      mp, (S *)L.out0, (S *)L.out1, p);
 }
 
 cudaError_t launch_tti(const K1Launch &L, cudaStream_t st) {
-    if (L.fp64) return L.tx == 4 ? launch_tti_t<4, double>(L, st) : launch_tti_t<8, double>(L, st);
-    switch (L.tx) {
-        case 4: return launch_tti_t<4, float>(L, st);
-        case 16: return launch_tti_t<16, float>(L, st);
-        default: return launch_tti_t<8, float>(L, st);
-    }
+    if (L.fp64) return launch_tti_t<8, double, 0>(L, st);
+    if (L.tx == 16) return L.deep ? launch_tti_t<16, float, 1>(L, st) : launch_tti_t<16, float, 0>(L, st);
+    return L.deep ? launch_tti_t<8, float, 1>(L, st) : launch_tti_t<8, float, 0>(L, st);
 }
 
 }  // namespace a3d

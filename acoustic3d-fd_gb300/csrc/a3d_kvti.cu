@@ -12,9 +12,9 @@ namespace a3d {
 
 // ===========================================================================
 // vti_vel: maps {P (HX), Q (HZ), u, v, w (core), rho (core float)}
-template <int TX, class S>
+template <int TX, class S, int D>
 struct VtiVelL {
-    static constexpr int KA = 8, KB = 4;
+    static constexpr int KA = Depth<D>::KA, KB = Depth<D>::KB;
     static constexpr uint32_t C = 32 * TX, PX = 32 * (TX + 8), QZ = 40 * TX;
     static constexpr uint32_t A_BYTES = PX * sizeof(S);
     static constexpr uint32_t B_BYTES = (QZ + 3 * C) * sizeof(S) + C * 4;
@@ -24,11 +24,11 @@ struct VtiVelL {
     static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBars<KA, KB>);
 };
 
-template <int TX, class S>
+template <int TX, class S, int D>
 __global__ void __launch_bounds__(32 * TX + 32)
     vti_vel(const __grid_constant__ Maps<6> mp, S *__restrict__ u, S *__restrict__ v,
             S *__restrict__ w, const __grid_constant__ K1Params p) {
-    using L = VtiVelL<TX, S>;
+    using L = VtiVelL<TX, S, D>;
     using T = typename Arith<S>::T;
     constexpr int NC = 32 * TX;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -125,9 +125,9 @@ __global__ void __launch_bounds__(32 * TX + 32)
 
 // ===========================================================================
 // vti_stress: maps {v (core), u (HX), w (HZ), P, Q (core), rho, vp, eps, del (core float)}
-template <int TX, class S>
+template <int TX, class S, int D>
 struct VtiStrL {
-    static constexpr int KA = 8, KB = 4;
+    static constexpr int KA = Depth<D>::KA, KB = Depth<D>::KB;
     static constexpr uint32_t C = 32 * TX, UX = 32 * (TX + 8), WZ = 40 * TX;
     static constexpr uint32_t A_BYTES = C * sizeof(S);
     static constexpr uint32_t B_BYTES = (UX + WZ + 2 * C) * sizeof(S) + 4 * C * 4;
@@ -148,11 +148,11 @@ __device__ __forceinline__ void sv_eedd(const K1Params &p, int ix, int iy, int i
     dd = mul_df(del, t.x, t.y);
 }
 
-template <int TX, class S>
+template <int TX, class S, int D>
 __global__ void __launch_bounds__(32 * TX + 32)
     vti_stress(const __grid_constant__ Maps<9> mp, S *__restrict__ P, S *__restrict__ Q,
                const __grid_constant__ K1Params p) {
-    using L = VtiStrL<TX, S>;
+    using L = VtiStrL<TX, S, D>;
     using T = typename Arith<S>::T;
     constexpr int NC = 32 * TX;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -259,32 +259,29 @@ __global__ void __launch_bounds__(32 * TX + 32)
         });
 }
 
-template <int TX, class S>
+template <int TX, class S, int D>
 static cudaError_t launch_vti_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
     if (L.kind == K1_VTI_VEL) {
         static bool attr = false;
         Maps<6> mp;
         for (int i = 0; i < 6; ++i) mp.m[i] = L.maps[i];
-        const int grid = k1_sweep<TX>(p, vti_vel<TX, S>, 32 * TX + 32, VtiVelL<TX, S>::TOTAL, L.grid);
-        return k1_launch(vti_vel<TX, S>, 32 * TX + 32, VtiVelL<TX, S>::TOTAL, p.sw.W, grid, st, attr,
+        const int grid = k1_sweep<TX>(p, vti_vel<TX, S, D>, 32 * TX + 32, VtiVelL<TX, S, D>::TOTAL, L.grid, L.mode);
+        return k1_launch(vti_vel<TX, S, D>, 32 * TX + 32, VtiVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr,
                          mp, (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
     static bool attr = false;
     Maps<9> mp;
     for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
-    const int grid = k1_sweep<TX>(p, vti_stress<TX, S>, 32 * TX + 32, VtiStrL<TX, S>::TOTAL, L.grid);
-    return k1_launch(vti_stress<TX, S>, 32 * TX + 32, VtiStrL<TX, S>::TOTAL, p.sw.W, grid, st, attr,
+    const int grid = k1_sweep<TX>(p, vti_stress<TX, S, D>, 32 * TX + 32, VtiStrL<TX, S, D>::TOTAL, L.grid, L.mode);
+    return k1_launch(vti_stress<TX, S, D>, 32 * TX + 32, VtiStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr,
                      mp, (S *)L.out0, (S *)L.out1, p);
 }
 
 cudaError_t launch_vti(const K1Launch &L, cudaStream_t st) {
-    if (L.fp64) return L.tx == 4 ? launch_vti_t<4, double>(L, st) : launch_vti_t<8, double>(L, st);
-    switch (L.tx) {
-        case 4: return launch_vti_t<4, float>(L, st);
-        case 16: return launch_vti_t<16, float>(L, st);
-        default: return launch_vti_t<8, float>(L, st);
-    }
+    if (L.fp64) return launch_vti_t<8, double, 0>(L, st);
+    if (L.tx == 16) return L.deep ? launch_vti_t<16, float, 1>(L, st) : launch_vti_t<16, float, 0>(L, st);
+    return L.deep ? launch_vti_t<8, float, 1>(L, st) : launch_vti_t<8, float, 0>(L, st);
 }
 
 }  // namespace a3d

@@ -20,6 +20,13 @@
 
 namespace a3d {
 
+// ring depths: D = 0 — 8 A stages (4 live, 4 in flight) and 4 B stages;
+// D = 1 — 16 and 8, for more bytes in flight per CTA when fewer CTAs are resident
+template <int D> struct Depth {
+    static constexpr int KA = D ? 16 : 8;
+    static constexpr int KB = D ? 8 : 4;
+};
+
 template <int KA, int KB>
 struct PipeBars {
     uint64_t fullA[KA], emptyA[KA], fullB[KB], emptyB[KB];

@@ -102,7 +102,8 @@ typedef struct {
     int rec_z;         /* 2nd order: receiver depth in model cells; < 0: 1        */
     int mute;          /* zero the direct wave in the record                      */
     int storage;       /* enum a3d_storage of the wavefields (FP32 or FP64 here)  */
-    int tile_x;        /* kernel tile width along x (4, 8, 16); 0: default        */
+    int tile_x;        /* kernel tile width along x: 8 or 16 fixes it, 0 lets the
+                          autotuner choose, < 0 disables the autotuner (32x8 tiles) */
 } a3d_config;
 
 typedef struct {
@@ -148,6 +149,10 @@ int a3d_forward_host(const a3d_config *cfg, const float *vel, const float *rho, 
  * sweeps.  Turning profiling on resets the sums. */
 int a3d_engine_set_profiling(a3d_engine *e, int on);
 int a3d_engine_kernel_times(const a3d_engine *e, double *ms, long long *launches);
+
+/* JSON description of the engine (grid, layout, bytes held, the autotuned launch
+ * configuration of each kernel kind); runs the autotuner if it has not run. */
+int a3d_engine_describe(a3d_engine *e, char *buf, size_t n);
 
 /* Message of the last failure on the calling thread ("" if none). */
 const char *a3d_last_error(void);
