@@ -89,6 +89,10 @@ static int make_map(CUtensorMap *m, const void *base, bool f64, const Grid &g, i
     return A3D_OK;
 }
 
+int make_field_map(CUtensorMap *m, const void *base, bool f64, const Grid &g, int box0, int box1) {
+    return make_map(m, base, f64, g, box0, box1);
+}
+
 static int box_dims(int box, int tx, int &b0, int &b1) {
     b0 = (box == BOX_HZ || box == BOX_H) ? 40 : 32;
     b1 = (box == BOX_HX || box == BOX_H) ? tx + 8 : tx;

@@ -14,6 +14,9 @@ namespace a3d {
 int fail(int code, const char *fmt, ...);
 void clear_error();
 
+// tensor map over a padded field (dims nnz, nnx, nny; rows of g.ldz elements)
+int make_field_map(CUtensorMap *m, const void *base, bool f64, const Grid &g, int box0, int box1);
+
 // snapshot hook: want(it) says whether a snapshot is taken after step it;
 // take(it, window) receives the model window (nz*nx*ny floats, z fastest)
 struct SnapHook {

@@ -157,6 +157,40 @@ int a3d_engine_describe(a3d_engine *e, char *buf, size_t n);
 /* Message of the last failure on the calling thread ("" if none). */
 const char *a3d_last_error(void);
 
+/* ------------------------------------------- 2nd-order step without allocation */
+
+/* No counterpart in the reference.  One 2nd-order time step on device buffers the
+ * caller owns, for callers that cannot call cudaMalloc: a host framework that
+ * hands out all device memory from its own pool, or a process whose device memory
+ * is provisioned up front.  The call allocates nothing; the step kernel's scratch
+ * (three per-axis sponge-factor tables and an error word) lives in one fixed
+ * array of A3D_NOALLOC_SCRATCH_BYTES (about 97 KB) that every GPU which loads the
+ * library holds until the process exits.  Padded axes above A3D_NOALLOC_MAX_AXIS
+ * cells are rejected with A3D_E_ARG.
+ *
+ * Buffers (device, float, 16-byte aligned): the padded grid has nnz = nz + 8 +
+ * 2*npd cells along z (likewise x, y) and element (iz, ix, iy) at
+ * iz + ldz*(ix + nnx*iy), ldz >= nnz a multiple of 4.  `cur` is the current level
+ * including this step's dipole (before the first step set cur at the source cell
+ * (sz+4+npd, sx+4+npd, sy+4+npd) to w[0] and two cells deeper to -w[0]);
+ * `prev_next` holds the previous level on entry and the next level on return,
+ * with the next step's dipole amplitude w_next already added, so the two buffers
+ * swap roles every step.  `vv` is (v dt)^2 edge-padded.  `rec` ([ny][nx][nt]
+ * floats, receivers at model depth rec_z) receives sample `it`, or is NULL.
+ * The computation is the engine's 2nd-order step, bit for bit.
+ *
+ * The first call on a device sets up the scratch address for that device; make
+ * it before any stream capture.  Every call runs on the legacy default stream and
+ * waits for the step to finish.  All calls share the scratch array (tables
+ * recomputed and error word cleared on each call), so calls that overlap on the
+ * GPU — from several host threads, say — race. */
+#define A3D_NOALLOC_MAX_AXIS 4096
+#define A3D_NOALLOC_SCRATCH_BYTES (256 + 3 * A3D_NOALLOC_MAX_AXIS * 8)
+int a3d_2order_step_noalloc(const float *cur, float *prev_next, const float *vv, float *rec,
+                            int nx, int ny, int nz, int npd, int ldz, float dx, float dy,
+                            float dz, int sx, int sy, int sz, float w_next, int rec_z, int it,
+                            int nt, int device);
+
 #ifdef __cplusplus
 }
 #endif
