@@ -131,7 +131,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // complete within WAIT_CYCLES, or if another role already aborted (*abort != 0).
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code,
                                           volatile int *abort) {
-    if (mbar_try_wait(bar, parity)) return true;
+    // fast path: plain retries (try_wait suspends the warp for a while on each)
+    for (int i = 0; i < 64; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (true) {
         if (mbar_try_wait(bar, parity)) return true;

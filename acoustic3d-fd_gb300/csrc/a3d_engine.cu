@@ -207,7 +207,12 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
 
     // 1st-order engines
     if ((rc = upload_model(e, vel, &e->vp, tmp))) return rc;
-    if (c.physics != A3D_TTI && (rc = upload_model(e, rho, &e->rho, tmp))) return rc;
+    if (c.physics != A3D_TTI) {
+        if ((rc = upload_model(e, rho, &e->rho, tmp))) return rc;
+        // the velocity sweeps multiply by 1/rho (float reciprocal); the padding is 0
+        for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = tmp[i] != 0.0f ? 1.0f / tmp[i] : 0.0f;
+        if ((rc = upload_image(e, tmp, &e->rinv))) return rc;
+    }
     if (c.physics != A3D_ISO) {
         if ((rc = upload_model(e, eps, &e->eps, tmp))) return rc;
         if ((rc = upload_model(e, del, &e->del, tmp))) return rc;
@@ -248,6 +253,20 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     for (int a = 0; a < 3; ++a) {
         pml_profile(c.dt, d0, n3[a], e->npml, q, q + nn3[a], q + 2 * nn3[a], q + 3 * nn3[a]);
         q += 4 * nn3[a];
+    }
+    {   // pressure-undamped interval of each axis (x, y, z)
+        const float *qa = pm.data();
+        for (int a = 0; a < 3; ++a) {
+            const float *a1 = qa + 2 * nn3[a], *a2 = qa + 3 * nn3[a];
+            int lo = nn3[a], hi = 0;
+            for (int i = 0; i < nn3[a]; ++i)
+                if (a1[i] == 1.0f && a2[i] == 1.0f) { lo = std::min(lo, i); hi = std::max(hi, i + 1); }
+            for (int i = lo; i < hi; ++i)  // the interval must be contiguous
+                if (!(a1[i] == 1.0f && a2[i] == 1.0f)) return fail(A3D_E_ARG, "PML profile not contiguous");
+            e->ulo[a] = lo;
+            e->uhi[a] = hi;
+            qa += 4 * nn3[a];
+        }
     }
     e->pml = (float *)e->dalloc(pm.size() * 4);
     if (!e->pml) return fail(A3D_E_NOMEM, "device allocation failed");
@@ -292,18 +311,20 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
         e->nvel = 5;
         if ((rc = mk(&mvel[0], e->P, true, BOX_H)) || (rc = mk(&mvel[1], e->u, true, BOX_CORE)) ||
             (rc = mk(&mvel[2], e->v, true, BOX_CORE)) || (rc = mk(&mvel[3], e->w, true, BOX_CORE)) ||
-            (rc = mk(&mvel[4], e->rho, false, BOX_CORE)))
+            (rc = mk(&mvel[4], e->rinv, false, BOX_CORE)))
             return rc;
-        e->nstr = 6;
+        e->nstr = 9;
         if ((rc = mk(&mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&mstr[1], e->u, true, BOX_HX)) ||
             (rc = mk(&mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&mstr[3], e->P, true, BOX_CORE)) ||
-            (rc = mk(&mstr[4], e->rho, false, BOX_CORE)) || (rc = mk(&mstr[5], e->vp, false, BOX_CORE)))
+            (rc = mk(&mstr[4], e->rho, false, BOX_CORE)) || (rc = mk(&mstr[5], e->vp, false, BOX_CORE)) ||
+            (rc = mk(&mstr[6], e->px, true, BOX_CORE)) || (rc = mk(&mstr[7], e->py, true, BOX_CORE)) ||
+            (rc = mk(&mstr[8], e->pz, true, BOX_CORE)))
             return rc;
     } else if (c.physics == A3D_VTI) {
         e->nvel = 6;
         if ((rc = mk(&mvel[0], e->P, true, BOX_HX)) || (rc = mk(&mvel[1], e->Q, true, BOX_HZ)) ||
             (rc = mk(&mvel[2], e->u, true, BOX_CORE)) || (rc = mk(&mvel[3], e->v, true, BOX_CORE)) ||
-            (rc = mk(&mvel[4], e->w, true, BOX_CORE)) || (rc = mk(&mvel[5], e->rho, false, BOX_CORE)))
+            (rc = mk(&mvel[4], e->w, true, BOX_CORE)) || (rc = mk(&mvel[5], e->rinv, false, BOX_CORE)))
             return rc;
         e->nstr = 9;
         if ((rc = mk(&mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&mstr[1], e->u, true, BOX_HX)) ||
@@ -362,13 +383,19 @@ int a3d_engine::autotune() {
     const a3d_config &c = cfg;
     std::vector<Tune> cand;
     const int fixed_tx = c.tile_x == 8 || c.tile_x == 16 ? c.tile_x : 0;
+    // (tile width, rows per warp): the 2nd-order and isotropic kernels share tile
+    // rows among a warp's lanes; the VTI/TTI kernels use one row per warp
+    const bool multirow = c.physics == A3D_2ORDER || c.physics == A3D_ISO;
+    std::vector<std::pair<int, int>> shapes;
+    if (multirow) shapes = {{8, 1}, {16, 1}, {8, 2}, {16, 2}, {16, 4}};
+    else shapes = {{8, 1}, {16, 1}};
     if (c.tile_x < 0 || fp64) {  // fixed defaults (and the FP64 run): 32x8, shallow rings, both plans
-        for (int m = 0; m < 2; ++m) cand.push_back(Tune{8, false, m});
+        for (int m = 0; m < 2; ++m) cand.push_back(Tune{8, false, m, multirow ? 2 : 1});
     } else {
-        for (int tx : {8, 16})
+        for (auto sh : shapes)
             for (int d = 0; d < 2; ++d)
                 for (int m = 0; m < 2; ++m)
-                    if (!fixed_tx || tx == fixed_tx) cand.push_back(Tune{tx, d != 0, m});
+                    if (!fixed_tx || sh.first == fixed_tx) cand.push_back(Tune{sh.first, d != 0, m, sh.second});
     }
     const int kinds = c.physics == A3D_2ORDER ? 1 : 2;
     cudaEvent_t t0, t1;
@@ -381,7 +408,7 @@ int a3d_engine::autotune() {
             auto launch_once = [&]() -> cudaError_t {
                 if (c.physics == A3D_2ORDER) {
                     K2OLaunch L{};
-                    L.tx = tc.tx; L.deep = tc.deep; L.mode = tc.mode; L.fp64 = fp64;
+                    L.tx = tc.tx; L.deep = tc.deep; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
                     L.tm_cur = m2o_cur[ti][0]; L.tm_prev = m2o_prev[ti][1]; L.tm_vv = m2o_vv[ti];
                     L.ybuf = Y;
                     K2OParams &p = L.p;
@@ -405,13 +432,14 @@ int a3d_engine::autotune() {
                 p.s_x = p.s_y = p.s_z = -100;
                 p.taper = taper;
                 p.px = px; p.py = py; p.pz = pz; p.qx = qx; p.qy = qy; p.qz = qz;
+                for (int a = 0; a < 3; ++a) { p.ulo[a] = ulo[a]; p.uhi[a] = uhi[a]; }
                 p.rec = rec; p.nt = c.nt; p.err = d_err;
                 const int kv = c.physics == A3D_ISO ? K1_ISO_VEL : (c.physics == A3D_VTI ? K1_VTI_VEL : K1_TTI_VEL);
                 L.kind = kv + k;
                 L.maps = k == 0 ? mvel[ti] : mstr[ti];
                 L.nmaps = k == 0 ? nvel : nstr;
                 L.out0 = k == 0 ? u : P; L.out1 = k == 0 ? v : Q; L.out2 = w;
-                L.tx = tc.tx; L.deep = tc.deep; L.mode = tc.mode; L.fp64 = fp64;
+                L.tx = tc.tx; L.deep = tc.deep; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
                 auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
                 return launch(L, st);
             };
@@ -489,6 +517,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         L.tx = tune[0].tx;
         L.deep = tune[0].deep;
         L.mode = tune[0].mode;
+        L.rows = tune[0].rows;
         L.fp64 = fp64;
         L.grid = 0;
         L.tm_vv = m2o_vv[ti];
@@ -539,6 +568,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         p.s_x = s.sx + np - 1; p.s_y = s.sy + np - 1; p.s_z = s.sz + np - 1;  // ..iso..:91-93
         p.taper = taper;
         p.px = px; p.py = py; p.pz = pz; p.qx = qx; p.qy = qy; p.qz = qz;
+        for (int a = 0; a < 3; ++a) { p.ulo[a] = ulo[a]; p.uhi[a] = uhi[a]; }
         p.rec = rec_dev;
         p.mute_nt = c.mute ? d_mute : nullptr;
         p.nt = c.nt;
@@ -549,8 +579,8 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         Ls.maps = mstr[tune[1].tx == 16 ? 1 : 0]; Ls.nmaps = nstr;
         Lv.out0 = u; Lv.out1 = v; Lv.out2 = w;
         Ls.out0 = P; Ls.out1 = Q;
-        Lv.tx = tune[0].tx; Lv.deep = tune[0].deep; Lv.mode = tune[0].mode;
-        Ls.tx = tune[1].tx; Ls.deep = tune[1].deep; Ls.mode = tune[1].mode;
+        Lv.tx = tune[0].tx; Lv.deep = tune[0].deep; Lv.mode = tune[0].mode; Lv.rows = tune[0].rows;
+        Ls.tx = tune[1].tx; Ls.deep = tune[1].deep; Ls.mode = tune[1].mode; Ls.rows = tune[1].rows;
         Lv.fp64 = Ls.fp64 = fp64; Lv.grid = Ls.grid = 0;
         auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
         if ((rc = prepare_profiling(this, 3))) return rc;
@@ -733,10 +763,11 @@ extern "C" int a3d_engine_describe(a3d_engine *e, char *buf, size_t n) {
     }
     snprintf(buf, n,
              "{\"grid\": [%d, %d, %d], \"ldz\": %d, \"pad\": %d, \"device_bytes\": %zu, "
-             "\"kernels\": [{\"tile_x\": %d, \"deep\": %d, \"plan\": %d, \"ms\": %.4f}, "
-             "{\"tile_x\": %d, \"deep\": %d, \"plan\": %d, \"ms\": %.4f}]}",
-             e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, e->tune[0].tx, (int)e->tune[0].deep,
-             e->tune[0].mode, e->tune[0].ms, e->tune[1].tx, (int)e->tune[1].deep, e->tune[1].mode, e->tune[1].ms);
+             "\"kernels\": [{\"tile_x\": %d, \"rows\": %d, \"deep\": %d, \"plan\": %d, \"ms\": %.4f}, "
+             "{\"tile_x\": %d, \"rows\": %d, \"deep\": %d, \"plan\": %d, \"ms\": %.4f}]}",
+             e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, e->tune[0].tx, e->tune[0].rows,
+             (int)e->tune[0].deep, e->tune[0].mode, e->tune[0].ms, e->tune[1].tx, e->tune[1].rows,
+             (int)e->tune[1].deep, e->tune[1].mode, e->tune[1].ms);
     return A3D_OK;
 }
 

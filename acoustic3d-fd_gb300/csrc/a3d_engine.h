@@ -41,7 +41,7 @@ struct a3d_engine {
     size_t dev_bytes = 0;
 
     // model parameters on the device (float, padded layout)
-    float *vv = nullptr, *vp = nullptr, *rho = nullptr, *eps = nullptr, *del = nullptr;
+    float *vv = nullptr, *vp = nullptr, *rho = nullptr, *rinv = nullptr, *eps = nullptr, *del = nullptr;
     float *tct = nullptr, *tst = nullptr, *tcp = nullptr, *tsp = nullptr;  // TTI trig
     float v_mute = 0.0f;   // direct-wave mute velocity
 
@@ -53,6 +53,7 @@ struct a3d_engine {
     // coefficients
     float2 *fz = nullptr, *fx = nullptr, *fy = nullptr;       // 2nd-order sponge
     float *pml = nullptr;  // cx1 cx2 ax1 ax2 | cy1 cy2 ay1 ay2 | cz1 cz2 az1 az2 blocks
+    int ulo[3] = {0, 0, 0}, uhi[3] = {0, 0, 0};  // pressure-undamped interval per axis (x, y, z)
     float2 *taper = nullptr;
     std::vector<float> w2o;                    // 2nd-order Ricker samples
     std::vector<float> amp0, amp1;             // 1st-order injected amplitudes per step
@@ -70,7 +71,7 @@ struct a3d_engine {
 
     // launch configuration per kernel kind ([0] velocity / 2nd-order step, [1] stress),
     // chosen by the autotuner on the first run unless fixed by the config
-    struct Tune { int tx = 8; bool deep = false; int mode = 0; float ms = 0; };
+    struct Tune { int tx = 8; bool deep = false; int mode = 0; int rows = 2; float ms = 0; };
     Tune tune[2];
     bool tuned = false;
     int autotune();

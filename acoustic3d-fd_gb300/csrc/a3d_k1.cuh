@@ -17,8 +17,10 @@ struct K1Params {
     int inj;                 // inject this step (t <= 2/fm)
     float amp0, amp1;        // isotropic: added at s_z and at s_z+2; VTI/TTI: added to P and Q
     const float2 *taper;     // SV ball: hi/lo of the epsilon/delta factor for r^2 = 0..225
-    // split (PML) components, touched only on damped axes
+    // split (PML) components, touched only on damped axes; pressure-undamped
+    // interval per axis (x, y, z): index i is undamped iff ulo <= i < uhi
     void *px, *py, *pz, *qx, *qy, *qz;
+    int ulo[3], uhi[3];
     // record at model depth 0 (padded z = npml)
     float *rec;
     const int *mute_nt;
@@ -41,6 +43,7 @@ struct K1Launch {
     bool fp64;
     bool deep;  // deep TMA rings
     int mode;   // sweep plan (plan_sweep)
+    int rows;   // tile rows per consumer warp (iso: 2 or 4; VTI/TTI: 1)
 };
 
 cudaError_t launch_k1(const K1Launch &L, cudaStream_t st);

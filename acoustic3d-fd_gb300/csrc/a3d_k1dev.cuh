@@ -37,6 +37,30 @@ __device__ __forceinline__ T pupdate(T Pold, T gx, T gy, T gz, bool dx, bool dy,
 
 __device__ __forceinline__ bool damped(float a1, float a2) { return !(a1 == 1.0f && a2 == 1.0f); }
 
+// pupdate on split components already in registers (prefetched); the new
+// components come back in cx, cy, cz for the caller to store
+template <class T>
+__device__ __forceinline__ T pupdate_r(T Pold, T gx, T gy, T gz, bool dx, bool dy, bool dz, float ax2,
+                                       float ay2, float az2, T &cx, T &cy, T &cz) {
+    if (!(dx | dy | dz)) return ((Pold - gx) - gy) - gz;
+    T s = Pold;
+    if (dx) s = s - cx;
+    if (dy) s = s - cy;
+    if (dz) s = s - cz;
+    if (!dx) s = s - gx;
+    if (!dy) s = s - gy;
+    if (!dz) s = s - gz;
+    if (dx) { cx = fma_t((T)ax2, cx, -gx); s = s + cx; }
+    if (dy) { cy = fma_t((T)ay2, cy, -gy); s = s + cy; }
+    if (dz) { cz = fma_t((T)az2, cz, -gz); s = s + cz; }
+    return s;
+}
+
+// does the tile [a0, a0+len) of an axis touch its damped region?
+__device__ __forceinline__ bool range_damped(int a0, int len, int lo, int hi) {
+    return a0 < lo || a0 + len > hi;
+}
+
 
 // launch helper: sets the smem attribute once, sizes the grid, launches
 template <class Kern, class... Args>

@@ -38,25 +38,25 @@ struct K2OSmem {
     static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBars<KA, KB>);
 };
 
-template <int TX, class S, int D>
-__global__ void __launch_bounds__(32 * TX + 32)
+template <int TX, class S, int D, int R>
+__global__ void __launch_bounds__(32 * (TX / R) + 32)
     k2o_step(const __grid_constant__ CUtensorMap tm_cur, const __grid_constant__ CUtensorMap tm_prev,
              const __grid_constant__ CUtensorMap tm_vv, S *__restrict__ ybuf,
              const __grid_constant__ K2OParams p) {
     using L = K2OSmem<TX, S, D>;
     using T = typename Arith<S>::T;
-    constexpr int NC = 32 * TX;  // consumer threads
+    constexpr int NW = TX / R;  // consumer warps, R tile rows each
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<PipeBars<L::KA, L::KB> *>(smem + L::BAR_OFF);
     unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
-    if (threadIdx.x == 0) bars.init(NC);
+    if (threadIdx.x == 0) bars.init(NW);
     __syncthreads();
     long long w0, w1;
     cta_range(p.sw, w0, w1);
     if (w0 >= w1) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    if (warp == TX) {
+    if (warp == NW) {
         if (lane != 0) return;
         prefetch_tmap(&tm_cur);
         prefetch_tmap(&tm_prev);
@@ -74,74 +74,95 @@ __global__ void __launch_bounds__(32 * TX + 32)
         return;
     }
 
-    const int tx = warp, tz = lane;
-    T win[9];  // current level at planes q-8 .. q (own column)
+    const int tz = lane, xw = warp * R;
+    T win[R][9];  // current level at planes q-8 .. q, per row
 #pragma unroll
-    for (int i = 0; i < 9; ++i) win[i] = T(0);
-    int iz = 0, ix = 0;
-    bool active = false, rec_row = false;
-    float2 fz{0.f, 0.f}, fx{0.f, 0.f};
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int i = 0; i < 9; ++i) win[r][i] = T(0);
+    int iz = 0;
+    bool zact = false, act[R], rec[R];
+    int ixr[R];
+    float2 fz{0.f, 0.f}, fx[R];
     const T k1 = (T)S8_1, k2 = (T)S8_2, k3 = (T)S8_3, k4 = (T)S8_4;
+    const size_t pstride = (size_t)p.ldz * p.nnx;
     pipe_consume<TX, L::KA, L::KB>(
         p.sw, w0, w1, bars, ringA, L::A_STRIDE, ringB, L::B_STRIDE, p.err,
         [&](const Seg &s) {
             iz = s.z0 + tz;
-            ix = s.x0 + tx;
-            active = iz < p.nnz - MM && ix < p.nnx - MM;
+            zact = iz < p.nnz - MM;
             // sponge factors of this column (hi == 0: no sponge on that face)
             fz = p.fz[min(iz, p.nnz - 1)];
-            fx = p.fx[min(ix, p.nnx - 1)];
-            rec_row = iz == p.gz && ix >= p.rx0 && ix < p.rx0 + p.nx;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int ix = s.x0 + xw + r;
+                ixr[r] = ix;
+                act[r] = zact && ix < p.nnx - MM;
+                fx[r] = p.fx[min(ix, p.nnx - 1)];
+                rec[r] = iz == p.gz && ix >= p.rx0 && ix < p.rx0 + p.nx;
+            }
         },
         [&](unsigned char *st, const Seg &, int) {
             const S *At = reinterpret_cast<const S *>(st);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) win[i] = win[i + 1];
-            win[8] = (T)At[(tx + MM) * L::AW + tz + MM];
+            for (int r = 0; r < R; ++r) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) win[r][i] = win[r][i + 1];
+                win[r][8] = (T)At[(xw + r + MM) * L::AW + tz + MM];
+            }
         },
         [&](unsigned char *sa, unsigned char *sb, const Seg &, int o) {
-            if (!active) return;
+            if (!zact) return;
             const S *Ao = reinterpret_cast<const S *>(sa);
             const S *Bp = reinterpret_cast<const S *>(sb);
             const float *Bv = reinterpret_cast<const float *>(sb + L::B_BYTES);
             const float2 fy = p.fy[o];
-            const int c = (tx + MM) * L::AW + tz + MM, bi = tx * 32 + tz;
-            const T cur = win[4];
-            T c1 = (T)S8_0 * cur, c2 = c1, c3 = c1;
-            // z, x from the tile; y from the register window (2O:284-289)
-            c1 = fma_t(k1, (T)Ao[c - 1] + (T)Ao[c + 1], c1);
-            c2 = fma_t(k1, (T)Ao[c - L::AW] + (T)Ao[c + L::AW], c2);
-            c3 = fma_t(k1, win[5] + win[3], c3);
-            c1 = fma_t(k2, (T)Ao[c - 2] + (T)Ao[c + 2], c1);
-            c2 = fma_t(k2, (T)Ao[c - 2 * L::AW] + (T)Ao[c + 2 * L::AW], c2);
-            c3 = fma_t(k2, win[6] + win[2], c3);
-            c1 = fma_t(k3, (T)Ao[c - 3] + (T)Ao[c + 3], c1);
-            c2 = fma_t(k3, (T)Ao[c - 3 * L::AW] + (T)Ao[c + 3 * L::AW], c2);
-            c3 = fma_t(k3, win[7] + win[1], c3);
-            c1 = fma_t(k4, (T)Ao[c - 4] + (T)Ao[c + 4], c1);
-            c2 = fma_t(k4, (T)Ao[c - 4 * L::AW] + (T)Ao[c + 4 * L::AW], c2);
-            c3 = fma_t(k4, win[8] + win[0], c3);
-            c1 *= (T)p.dz2;
-            c2 *= (T)p.dx2;
-            c3 *= (T)p.dy2;
-            const T m = (T)Bv[bi] * ((c1 + c2) + c3);
-            const T prev = sponge3<T>((T)Bp[bi], fy, fx, fz);
-            T nxt;
-            if constexpr (sizeof(T) == 4)
-                nxt = upd2o(cur, prev, m);
-            else
-                nxt = (T(2) * cur - prev) + m;
-            nxt = sponge3<T>(nxt, fy, fx, fz);
-            if (ix == p.s_x && o == p.s_y) {  // next step's dipole (2O:184-185)
-                if (iz == p.s_z) nxt = nxt + (T)p.w_next;
-                if (iz == p.s_z + 2) nxt = nxt - (T)p.w_next;
-            }
-            ybuf[(size_t)iz + (size_t)p.ldz * ((size_t)ix + (size_t)p.nnx * o)] = to_store<S, T>(nxt);
-            if (rec_row && o >= p.ry0 && o < p.ry0 + p.ny) {  // cuda_record after absorb (2O:452)
-                const size_t tr = (size_t)(ix - p.rx0) + (size_t)p.nx * (o - p.ry0);
-                T r = sponge3<T>(cur, fy, fx, fz);
-                if (p.mute_nt && p.it < p.mute_nt[tr]) r = T(0);
-                p.rec[tr * p.nt + p.it] = (float)r;
+            // current level at tile rows xw .. xw+R+7 of this z column: xs[j] = cur(x = xw - 4 + j)
+            T xs[R + 8];
+#pragma unroll
+            for (int j = 0; j < R + 8; ++j) xs[j] = (T)Ao[(xw + j) * L::AW + tz + MM];
+            const size_t po = pstride * o;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (!act[r]) continue;
+                const int c = (xw + r + MM) * L::AW + tz + MM, bi = (xw + r) * 32 + tz;
+                const T cur = win[r][4];
+                T c1 = (T)S8_0 * cur, c2 = c1, c3 = c1;
+                // z from the tile, x from the shared rows, y from the window (2O:284-289)
+                c1 = fma_t(k1, (T)Ao[c - 1] + (T)Ao[c + 1], c1);
+                c2 = fma_t(k1, xs[r + 3] + xs[r + 5], c2);
+                c3 = fma_t(k1, win[r][5] + win[r][3], c3);
+                c1 = fma_t(k2, (T)Ao[c - 2] + (T)Ao[c + 2], c1);
+                c2 = fma_t(k2, xs[r + 2] + xs[r + 6], c2);
+                c3 = fma_t(k2, win[r][6] + win[r][2], c3);
+                c1 = fma_t(k3, (T)Ao[c - 3] + (T)Ao[c + 3], c1);
+                c2 = fma_t(k3, xs[r + 1] + xs[r + 7], c2);
+                c3 = fma_t(k3, win[r][7] + win[r][1], c3);
+                c1 = fma_t(k4, (T)Ao[c - 4] + (T)Ao[c + 4], c1);
+                c2 = fma_t(k4, xs[r] + xs[r + 8], c2);
+                c3 = fma_t(k4, win[r][8] + win[r][0], c3);
+                c1 *= (T)p.dz2;
+                c2 *= (T)p.dx2;
+                c3 *= (T)p.dy2;
+                const T m = (T)Bv[bi] * ((c1 + c2) + c3);
+                const T prev = sponge3<T>((T)Bp[bi], fy, fx[r], fz);
+                T nxt;
+                if constexpr (sizeof(T) == 4)
+                    nxt = upd2o(cur, prev, m);
+                else
+                    nxt = (T(2) * cur - prev) + m;
+                nxt = sponge3<T>(nxt, fy, fx[r], fz);
+                if (ixr[r] == p.s_x && o == p.s_y) {  // next step's dipole (2O:184-185)
+                    if (iz == p.s_z) nxt = nxt + (T)p.w_next;
+                    if (iz == p.s_z + 2) nxt = nxt - (T)p.w_next;
+                }
+                ybuf[(size_t)iz + (size_t)p.ldz * ixr[r] + po] = to_store<S, T>(nxt);
+                if (rec[r] && o >= p.ry0 && o < p.ry0 + p.ny) {  // cuda_record after absorb (2O:452)
+                    const size_t tr = (size_t)(ixr[r] - p.rx0) + (size_t)p.nx * (o - p.ry0);
+                    T rr = sponge3<T>(cur, fy, fx[r], fz);
+                    if (p.mute_nt && p.it < p.mute_nt[tr]) rr = T(0);
+                    p.rec[tr * p.nt + p.it] = (float)rr;
+                }
             }
         });
 }
@@ -149,10 +170,11 @@ __global__ void __launch_bounds__(32 * TX + 32)
 // ---------------------------------------------------------------------------
 // host launcher
 
-template <int TX, class S, int D>
+template <int TX, class S, int D, int R>
 static cudaError_t launch_k2o_t(const K2OLaunch &L, cudaStream_t st) {
     using SM = K2OSmem<TX, S, D>;
-    auto kern = k2o_step<TX, S, D>;
+    auto kern = k2o_step<TX, S, D, R>;
+    constexpr int NT = 32 * (TX / R) + 32;
     static bool attr_done = false;
     if (!attr_done) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -166,18 +188,24 @@ static cudaError_t launch_k2o_t(const K2OLaunch &L, cudaStream_t st) {
     p.sw.y_begin = MM;
     p.sw.NY = p.nny - 2 * MM;
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * TX + 32, SM::TOTAL);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, SM::TOTAL);
     int grid = plan_sweep(p.sw, occ, L.mode);
     if (L.grid > 0) grid = L.grid;
-    kern<<<grid, 32 * TX + 32, SM::TOTAL, st>>>(L.tm_cur, L.tm_prev, L.tm_vv,
+    kern<<<grid, NT, SM::TOTAL, st>>>(L.tm_cur, L.tm_prev, L.tm_vv,
                                                 reinterpret_cast<S *>(L.ybuf), p);
     return cudaGetLastError();
 }
 
+// configurations: (tile width, rows per warp) in {8, 16} x {1, 2} and (16, 4), two ring depths
 cudaError_t launch_k2o(const K2OLaunch &L, cudaStream_t st) {
-    if (L.fp64) return launch_k2o_t<8, double, 0>(L, st);
-    if (L.tx == 16) return L.deep ? launch_k2o_t<16, float, 1>(L, st) : launch_k2o_t<16, float, 0>(L, st);
-    return L.deep ? launch_k2o_t<8, float, 1>(L, st) : launch_k2o_t<8, float, 0>(L, st);
+    if (L.fp64) return launch_k2o_t<8, double, 0, 2>(L, st);
+    if (L.tx == 16) {
+        if (L.rows == 4) return L.deep ? launch_k2o_t<16, float, 1, 4>(L, st) : launch_k2o_t<16, float, 0, 4>(L, st);
+        if (L.rows == 1) return L.deep ? launch_k2o_t<16, float, 1, 1>(L, st) : launch_k2o_t<16, float, 0, 1>(L, st);
+        return L.deep ? launch_k2o_t<16, float, 1, 2>(L, st) : launch_k2o_t<16, float, 0, 2>(L, st);
+    }
+    if (L.rows == 1) return L.deep ? launch_k2o_t<8, float, 1, 1>(L, st) : launch_k2o_t<8, float, 0, 1>(L, st);
+    return L.deep ? launch_k2o_t<8, float, 1, 2>(L, st) : launch_k2o_t<8, float, 0, 2>(L, st);
 }
 
 size_t k2o_smem_bytes(int tx, bool fp64) {

@@ -58,6 +58,7 @@ struct K2OLaunch {
     bool fp64;
     bool deep;   // deep TMA rings (16 + 8 stages) instead of 8 + 4
     int mode;    // sweep plan (plan_sweep)
+    int rows;    // tile rows per consumer warp (2 or 4)
 };
 
 cudaError_t launch_k2o(const K2OLaunch &L, cudaStream_t st);

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(32 * TX + 32)
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<PipeBars<L::KA, L::KB> *>(smem + L::BAR_OFF);
     unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
-    if (threadIdx.x == 0) bars.init(NC);
+    if (threadIdx.x == 0) bars.init(NC / 32);
     __syncthreads();
     long long w0, w1;
     cta_range(p.sw, w0, w1);
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(32 * TX + 32)
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<PipeBars<L::KA, L::KB> *>(smem + L::BAR_OFF);
     unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
-    if (threadIdx.x == 0) bars.init(NC);
+    if (threadIdx.x == 0) bars.init(NC / 32);
     __syncthreads();
     long long w0, w1;
     cta_range(p.sw, w0, w1);

@@ -11,7 +11,7 @@
 namespace a3d {
 
 // ===========================================================================
-// vti_vel: maps {P (HX), Q (HZ), u, v, w (core), rho (core float)}
+// vti_vel: maps {P (HX), Q (HZ), u, v, w (core), 1/rho (core float)}
 template <int TX, class S, int D>
 struct VtiVelL {
     static constexpr int KA = Depth<D>::KA, KB = Depth<D>::KB;
@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(32 * TX + 32)
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<PipeBars<L::KA, L::KB> *>(smem + L::BAR_OFF);
     unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
-    if (threadIdx.x == 0) bars.init(NC);
+    if (threadIdx.x == 0) bars.init(NC / 32);
     __syncthreads();
     long long w0, w1;
     cta_range(p.sw, w0, w1);
@@ -111,10 +111,10 @@ __global__ void __launch_bounds__(32 * TX + 32)
                 xx = fma_t(k[im], ld<T>(A, ca + (im + 1) * 32) - ld<T>(A, ca - im * 32), xx);
                 zz = fma_t(k[im], ld<T>(Bq, cq + im + 1) - ld<T>(Bq, cq - im), zz);
             }
-            const T r = (T)Br[bi];
-            xx = xx / r;
-            yy = yy / r;
-            zz = zz / r;
+            const T ri = (T)Br[bi];  // 1/rho
+            xx = xx * ri;
+            yy = yy * ri;
+            zz = zz * ri;
             const T cy1 = (T)p.cy1[o], cy2 = (T)p.cy2[o];
             const size_t g = gidx<S>(p, iz, ix, o);
             u[g] = to_store<S, T>(fma_t(cx2, ld<T>(Bu, bi), -((cx1 * (T)p.dtx) * xx)));
@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(32 * TX + 32)
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<PipeBars<L::KA, L::KB> *>(smem + L::BAR_OFF);
     unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
-    if (threadIdx.x == 0) bars.init(NC);
+    if (threadIdx.x == 0) bars.init(NC / 32);
     __syncthreads();
     long long w0, w1;
     cta_range(p.sw, w0, w1);

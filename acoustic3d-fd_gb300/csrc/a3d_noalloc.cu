@@ -102,6 +102,7 @@ extern "C" int a3d_2order_step_noalloc(const float *cur, float *prev_next, const
     g.nnx = nnx; g.nny = nny; g.nnz = nnz; g.ldz = ldz;
     K2OLaunch L{};
     L.tx = 8;
+    L.rows = 2;
     L.fp64 = false;
     if ((rc = make_field_map(&L.tm_cur, cur, false, g, 40, L.tx + 8)) ||
         (rc = make_field_map(&L.tm_prev, prev_next, false, g, 32, L.tx)) ||

@@ -11,6 +11,8 @@
 //   A stage of item j is read at its own arrival (window push) and 4 items later
 //   (in-plane neighbours of output plane q-4), then released: KA >= 5.
 //   B stage is released right after the output plane is computed.
+//   Releases are per warp (the empty barriers count consumer warps): the warp
+//   converges, then its lane 0 arrives.
 //
 // Every wait is bounded (mbar_wait); a timeout records an error code, raises a
 // CTA-wide abort flag so the other role stops, and the producer drains all
@@ -31,7 +33,7 @@ template <int KA, int KB>
 struct PipeBars {
     uint64_t fullA[KA], emptyA[KA], fullB[KB], emptyB[KB];
     int abort_flag;
-    __device__ void init(int nconsumers) {
+    __device__ void init(int nconsumers) {  // nconsumers: consumer warps
         for (int i = 0; i < KA; ++i) { mbar_init(&fullA[i], 1); mbar_init(&emptyA[i], nconsumers); }
         for (int i = 0; i < KB; ++i) { mbar_init(&fullB[i], 1); mbar_init(&emptyB[i], nconsumers); }
         abort_flag = 0;
@@ -62,7 +64,8 @@ __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long 
 }
 
 // Producer: one thread.  issueA(stage_ptr, bar, seg, q) / issueB(stage_ptr, bar, seg, o)
-// issue the copies of one item (the expect_tx byte counts are bytesA / bytesB).
+// issue the copies of one item (the expect_tx byte counts are bytesA / bytesB; with
+// bytesB == 0 issueB posts its own expect_tx, for items whose size varies).
 template <int TX, int KA, int KB, class IssueA, class IssueB>
 __device__ __forceinline__ void pipe_produce(const Sweep &sw, long long w0, long long w1,
                                              PipeBars<KA, KB> &b, unsigned char *ringA,
@@ -90,7 +93,7 @@ __device__ __forceinline__ void pipe_produce(const Sweep &sw, long long w0, long
                 if (jb >= KB)
                     ok = mbar_wait(&b.emptyB[sb], ((jb / KB) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab);
                 if (!ok) break;
-                mbar_arrive_expect_tx(&b.fullB[sb], bytesB);
+                if (bytesB) mbar_arrive_expect_tx(&b.fullB[sb], bytesB);
                 issueB(ringB + sb * strideB, &b.fullB[sb], s, o);
                 ++jb;
             }
@@ -127,10 +130,12 @@ __device__ __forceinline__ bool pipe_consume(const Sweep &sw, long long w0, long
                 const uint32_t sb = jb % KB;
                 if (!mbar_wait(&b.fullB[sb], (jb / KB) & 1, err, KERR_FULL_TIMEOUT, ab)) return false;
                 onOut(ringA + ((ja - MM) % KA) * strideA, ringB + sb * strideB, s, o);
-                mbar_arrive(&b.emptyB[sb]);
+                __syncwarp();
+                if ((threadIdx.x & 31) == 0) mbar_arrive(&b.emptyB[sb]);
                 ++jb;
             }
-            if (ja >= MM) mbar_arrive(&b.emptyA[(ja - MM) % KA]);
+            __syncwarp();
+            if (ja >= MM && (threadIdx.x & 31) == 0) mbar_arrive(&b.emptyA[(ja - MM) % KA]);
             ++ja;
         }
         w = wend;

@@ -255,8 +255,11 @@ def main():
                           dz=cfgd["dz"], nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
                           rec_z=cfgd.get("rec_z", -1), tile_x=args.tile_x)
     e = a3d.Engine(cfg, models, device=dev)
-    # replicas: rank r shifts its shot along x
-    sx = min(cfgd["nx"] - 1, shot[0] + 4 * rank)
+    # replicas: the job's shots run along x, one per rank, split round-robin as
+    # the reference splits shots over nodes
+    import a3d_dist
+    job_shots = [(min(cfgd["nx"] - 1, shot[0] + 4 * k), shot[1], shot[2]) for k in range(ws)]
+    sx = a3d_dist.shots_for_rank(job_shots, rank, ws)[0][0]
     for _ in range(args.warmup):
         e.run_device(sx, shot[1], shot[2])
 
@@ -278,11 +281,8 @@ def main():
     barrier()
     kms, kn = e.kernel_times()
     e.set_profiling(False)
-    if group:
-        import torch
-        t = torch.tensor([dev_ms], dtype=torch.float64, device=f"cuda:{dev}")
-        group.all_reduce(t, op=group.ReduceOp.MAX)
-        dev_ms = float(t.item())
+    tuning = e.describe()["kernels"]
+    dev_ms = a3d_dist.max_over_ranks(dev_ms, group, f"cuda:{dev}" if group else None)
     cells = updated_cells(cfgd)
     nt = cfgd["nt"]
     value = cells * nt * args.steps * ws / (dev_ms / 1000.0) / 1e9
@@ -357,7 +357,7 @@ def main():
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": "Gpts/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "call": "a3d_forward_host"},
-                "wall_s_timed": wall, "clocks": clocks,
+                "wall_s_timed": wall, "clocks": clocks, "tuning": tuning,
                 "gpu_launches": int(kn[0] + kn[1])}
         print(json.dumps(line), flush=True)
     if group:

@@ -17,7 +17,8 @@
  *            source added into P and then overwritten).
  *   form 1 — "engine": the arithmetic of the CUDA engines (unsplit P/Q in the
  *            undamped interior, split components only on PML-damped axes,
- *            source injected into the velocity update's view of P only).
+ *            source injected into the velocity update's view of P only, the
+ *            velocity update multiplied by the float reciprocal of density).
  *            The CUDA kernels reproduce this form bit for bit.
  * For the 2nd-order engine the two forms coincide.
  *
