@@ -129,6 +129,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 
 // Bounded wait: returns false (and records `code` in *err) if the phase does not
 // complete within WAIT_CYCLES, or if another role already aborted (*abort != 0).
+// With abort == nullptr (the exit-time drain of in-flight copies) only the time
+// limit ends the wait: copies already issued must land before the CTA exits.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code,
                                           volatile int *abort) {
     // fast path: plain retries (try_wait suspends the warp for a while on each)
@@ -137,10 +139,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
     const long long t0 = clock64();
     while (true) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (*abort) return false;
+        if (abort && *abort) return false;
         if (clock64() - t0 > WAIT_CYCLES) {
             atomicCAS(err, 0, code);
-            *abort = 1;
+            if (abort) *abort = 1;
             return false;
         }
     }

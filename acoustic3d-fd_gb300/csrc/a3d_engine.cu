@@ -4,6 +4,7 @@
 #include <cudaTypedefs.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -389,6 +390,25 @@ int a3d_engine::autotune() {
     std::vector<std::pair<int, int>> shapes;
     if (multirow) shapes = {{8, 1}, {16, 1}, {8, 2}, {16, 2}, {16, 4}};
     else shapes = {{8, 1}, {16, 1}};
+    // A3D_TUNE="tx,rows,deep,plan[;tx,rows,deep,plan]" pins the launch configuration of
+    // each kernel kind (velocity; stress) instead of timing candidates
+    if (const char *env = getenv("A3D_TUNE"); env && *env && !fp64) {
+        const char *q = env;
+        for (int k = 0; k < 2; ++k) {
+            int tx = 0, rows = 0, deep = 0, mode = 0, n = 0;
+            if (sscanf(q, "%d,%d,%d,%d%n", &tx, &rows, &deep, &mode, &n) != 4 || (tx != 8 && tx != 16) ||
+                (rows != 1 && rows != 2 && rows != 4) || (rows == 4 && tx != 16) || mode < 0 || mode > 1)
+                return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,deep,plan[;...], got \"%s\"", env);
+            if (!multirow && rows != 1) return fail(A3D_E_ARG, "A3D_TUNE: this physics runs one row per warp");
+            tune[k] = Tune{tx, deep != 0, mode, rows};
+            tune[k].ms = 0;
+            q += n;
+            if (*q == ';') ++q;
+            else if (k == 0) { tune[1] = tune[0]; break; }
+        }
+        tuned = true;
+        return A3D_OK;
+    }
     if (c.tile_x < 0 || fp64) {  // fixed defaults (and the FP64 run): 32x8, shallow rings, both plans
         for (int m = 0; m < 2; ++m) cand.push_back(Tune{8, false, m, multirow ? 2 : 1});
     } else {
@@ -498,6 +518,38 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         CUDA_TRY(cudaStreamSynchronize(st));
         return hook->take ? hook->take(it, snap_host.data()) : A3D_OK;
     };
+    // the time loop, bracketed by ev0/ev1; with graph mode (and no snapshot or
+    // per-kernel events in the loop) it is captured into a CUDA graph first and the
+    // graph is launched once, so the steps go to the GPU as one submission
+    const bool use_graph = graph && !profiling && !(hook && hook->want);
+    auto time_loop = [&](auto &&loop) -> int {
+        if (!use_graph) {
+            CUDA_TRY(cudaEventRecord(ev0, st));
+            int r = loop();
+            if (r) return r;
+            CUDA_TRY(cudaEventRecord(ev1, st));
+            return A3D_OK;
+        }
+        CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+        const int r = loop();
+        cudaGraph_t gr = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(st, &gr);
+        if (r || ec != cudaSuccess) {
+            if (gr) cudaGraphDestroy(gr);
+            return r ? r : fail(A3D_E_CUDA, "stream capture of the time loop failed: %s", cudaGetErrorString(ec));
+        }
+        cudaGraphExec_t ge = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&ge, gr, 0);
+        cudaGraphDestroy(gr);
+        if (ei != cudaSuccess) return fail(A3D_E_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(ei));
+        cudaError_t el = cudaEventRecord(ev0, st);
+        if (el == cudaSuccess) el = cudaGraphLaunch(ge, st);
+        if (el == cudaSuccess) el = cudaEventRecord(ev1, st);
+        if (el == cudaSuccess) el = cudaStreamSynchronize(st);
+        cudaGraphExecDestroy(ge);
+        if (el != cudaSuccess) return fail(A3D_E_CUDA, "graph launch of the time loop failed: %s", cudaGetErrorString(el));
+        return A3D_OK;
+    };
     if (c.physics == A3D_2ORDER) {
         CUDA_TRY(cudaMemsetAsync(field_alloc(X, esz), 0, fb, st));
         CUDA_TRY(cudaMemsetAsync(field_alloc(Y, esz), 0, fb, st));
@@ -535,22 +587,25 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         p.nt = c.nt;
         p.err = d_err;
         void *buf[2] = {X, Y};
-        int cur = 0;
         if ((rc = prepare_profiling(this, 2))) return rc;
-        CUDA_TRY(cudaEventRecord(ev0, st));
-        for (int it = 0; it < c.nt; ++it) {
-            L.tm_cur = m2o_cur[ti][cur];
-            L.tm_prev = m2o_prev[ti][1 - cur];
-            L.ybuf = buf[1 - cur];
-            p.w_next = it + 1 < c.nt ? w2o[it + 1] : 0.0f;
-            p.it = it;
-            if (profiling) CUDA_TRY(cudaEventRecord(kev[2 * it], st));
-            CUDA_TRY(launch_k2o(L, st));
-            if (profiling) CUDA_TRY(cudaEventRecord(kev[2 * it + 1], st));
-            if ((rc = snapshot(it, buf[cur]))) return rc;
-            cur = 1 - cur;
-        }
-        CUDA_TRY(cudaEventRecord(ev1, st));
+        rc = time_loop([&]() -> int {
+            int cur = 0;
+            for (int it = 0; it < c.nt; ++it) {
+                L.tm_cur = m2o_cur[ti][cur];
+                L.tm_prev = m2o_prev[ti][1 - cur];
+                L.ybuf = buf[1 - cur];
+                p.w_next = it + 1 < c.nt ? w2o[it + 1] : 0.0f;
+                p.it = it;
+                if (profiling) CUDA_TRY(cudaEventRecord(kev[2 * it], st));
+                CUDA_TRY(launch_k2o(L, st));
+                if (profiling) CUDA_TRY(cudaEventRecord(kev[2 * it + 1], st));
+                int r2 = snapshot(it, buf[cur]);
+                if (r2) return r2;
+                cur = 1 - cur;
+            }
+            return A3D_OK;
+        });
+        if (rc) return rc;
     } else {
         void *fields[11] = {u, v, w, P, Q, px, py, pz, qx, qy, qz};
         for (void *f : fields)
@@ -584,22 +639,25 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         Lv.fp64 = Ls.fp64 = fp64; Lv.grid = Ls.grid = 0;
         auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
         if ((rc = prepare_profiling(this, 3))) return rc;
-        CUDA_TRY(cudaEventRecord(ev0, st));
-        for (int it = 0; it < c.nt; ++it) {
-            p.it = it;
-            p.inj = inj[it];
-            p.amp0 = amp0[it];
-            p.amp1 = amp1[it];
-            Lv.p = p;
-            Ls.p = p;
-            if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it], st));
-            CUDA_TRY(launch(Lv, st));
-            if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 1], st));
-            CUDA_TRY(launch(Ls, st));
-            if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 2], st));
-            if ((rc = snapshot(it, P))) return rc;
-        }
-        CUDA_TRY(cudaEventRecord(ev1, st));
+        rc = time_loop([&]() -> int {
+            for (int it = 0; it < c.nt; ++it) {
+                p.it = it;
+                p.inj = inj[it];
+                p.amp0 = amp0[it];
+                p.amp1 = amp1[it];
+                Lv.p = p;
+                Ls.p = p;
+                if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it], st));
+                CUDA_TRY(launch(Lv, st));
+                if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 1], st));
+                CUDA_TRY(launch(Ls, st));
+                if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 2], st));
+                int r2 = snapshot(it, P);
+                if (r2) return r2;
+            }
+            return A3D_OK;
+        });
+        if (rc) return rc;
     }
     if ((rc = check_kernel_error(this))) return rc;
     if (profiling) {
@@ -670,6 +728,11 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
         e->npml = cfg->npml > 0 ? cfg->npml : (ph == A3D_TTI ? 40 : 20);
         if (e->npml < 6) { delete e; return fail(A3D_E_ARG, "PML width %d below 6 cells", e->npml); }
         e->g.set(cfg->nx, cfg->ny, cfg->nz, e->npml);
+    }
+    if (e->g.elems() > (size_t)INT32_MAX) {  // kernels index a field with 32-bit offsets
+        const size_t n = e->g.elems();
+        delete e;
+        return fail(A3D_E_ARG, "padded grid of %zu cells exceeds 2^31 - 1", n);
     }
     if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) {

@@ -76,6 +76,10 @@ struct a3d_engine {
     bool tuned = false;
     int autotune();
 
+    // replay each shot's time loop as one CUDA graph (ignored with snapshots or
+    // per-kernel timing)
+    bool graph = false;
+
     // optional per-kernel timing: events around every launch of each kernel kind
     bool profiling = false;
     std::vector<cudaEvent_t> kev;  // 3 per step (1st order) or 2 per step (2nd order)

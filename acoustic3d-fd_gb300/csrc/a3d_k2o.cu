@@ -8,8 +8,9 @@
 //     z/x halo (TMA box {32+8, TX+8, 1}) into a ring of KA stages, and the raw
 //     previous level and vv = (v dt)^2 at the output plane (boxes {32, TX, 1})
 //     into a ring of KB stages.
-//   * Consumer warps (one 32-cell z row each) keep a 9-plane register window
-//     for the y-derivative and read the z/x neighbours from the halo'd tile.
+//   * Consumer warps (R tile rows each, lane = z) keep an 8-plane register
+//     window for the y-derivative (the 9th plane is read from its fresh tile)
+//     and read the z/x neighbours from the halo'd tile.
 //
 // State kept in two buffers X (current) and Y (previous, raw):
 //   prev   = sponge(Y)                          reference: absorb of p0 after swap
@@ -35,7 +36,7 @@ struct K2OSmem {
     static constexpr size_t A_STRIDE = (A_BYTES + 127) / 128 * 128;
     static constexpr size_t B_STRIDE = (B_BYTES + VV_BYTES + 127) / 128 * 128;
     static constexpr size_t BAR_OFF = KA * A_STRIDE + KB * B_STRIDE;
-    static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBars<KA, KB>);
+    static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBarsM<KA, KB>);
 };
 
 template <int TX, class S, int D, int R>
@@ -45,9 +46,9 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
              const __grid_constant__ K2OParams p) {
     using L = K2OSmem<TX, S, D>;
     using T = typename Arith<S>::T;
-    constexpr int NW = TX / R;  // consumer warps, R tile rows each
+    constexpr int NW = TX / R, AW = L::AW;  // consumer warps, R tile rows each
     extern __shared__ __align__(128) unsigned char smem[];
-    auto &bars = *reinterpret_cast<PipeBars<L::KA, L::KB> *>(smem + L::BAR_OFF);
+    auto &bars = *reinterpret_cast<PipeBarsM<L::KA, L::KB> *>(smem + L::BAR_OFF);
     unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
     if (threadIdx.x == 0) bars.init(NW);
     __syncthreads();
@@ -61,105 +62,122 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
         prefetch_tmap(&tm_cur);
         prefetch_tmap(&tm_prev);
         prefetch_tmap(&tm_vv);
-        pipe_produce<TX, L::KA, L::KB>(
-            p.sw, w0, w1, bars, ringA, L::A_STRIDE, L::A_BYTES, ringB, L::B_STRIDE,
-            L::B_BYTES + L::VV_BYTES, p.err,
-            [&](unsigned char *dst, uint64_t *bar, const Seg &s, int q) {
-                tma_load_3d(dst, &tm_cur, bar, s.z0 - MM, s.x0 - MM, q);
-            },
-            [&](unsigned char *dst, uint64_t *bar, const Seg &s, int o) {
-                tma_load_3d(dst, &tm_prev, bar, s.z0, s.x0, o);
-                tma_load_3d(dst + L::B_BYTES, &tm_vv, bar, s.z0, s.x0, o);
+        pipe_produce_m<TX, L::KA, L::KB>(
+            p.sw, w0, w1, bars, p.err, [&](uint32_t sa, int sb, uint64_t *bar, const Seg &s, int q) {
+                mbar_arrive_expect_tx(bar, L::A_BYTES + (sb >= 0 ? L::B_BYTES + L::VV_BYTES : 0u));
+                tma_load_3d(ringA + sa * L::A_STRIDE, &tm_cur, bar, s.z0 - MM, s.x0 - MM, q);
+                if (sb < 0) return;
+                unsigned char *dst = ringB + sb * L::B_STRIDE;
+                tma_load_3d(dst, &tm_prev, bar, s.z0, s.x0, q - MM);
+                tma_load_3d(dst + L::B_BYTES, &tm_vv, bar, s.z0, s.x0, q - MM);
             });
         return;
     }
 
     const int tz = lane, xw = warp * R;
-    T win[R][9];  // current level at planes q-8 .. q, per row
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-#pragma unroll
-        for (int i = 0; i < 9; ++i) win[r][i] = T(0);
+    const int c0 = (xw + MM) * AW + tz + MM;  // this thread's first cell in an A tile
+    // current level at the last 8 planes, slot = item mod 8; the 9th plane of the
+    // y-stencil (the newest, q) is read from its A tile before it enters the window
+    T win[R][8];
     int iz = 0;
-    bool zact = false, act[R], rec[R];
-    int ixr[R];
+    bool act[R], rec[R], srow[R];
+    int trb[R];
+    uint32_t gb[R];
     float2 fz{0.f, 0.f}, fx[R];
     const T k1 = (T)S8_1, k2 = (T)S8_2, k3 = (T)S8_3, k4 = (T)S8_4;
-    const size_t pstride = (size_t)p.ldz * p.nnx;
-    pipe_consume<TX, L::KA, L::KB>(
-        p.sw, w0, w1, bars, ringA, L::A_STRIDE, ringB, L::B_STRIDE, p.err,
+    const T dz2 = (T)p.dz2, dx2 = (T)p.dx2, dy2 = (T)p.dy2;
+    const uint32_t pstride = (uint32_t)p.ldz * (uint32_t)p.nnx;
+    pipe_run<TX, L::KA, L::KB, MM>(
+        p.sw, w0, w1, bars, p.err,
         [&](const Seg &s) {
             iz = s.z0 + tz;
-            zact = iz < p.nnz - MM;
+            const bool zact = iz < p.nnz - MM;
             // sponge factors of this column (hi == 0: no sponge on that face)
             fz = p.fz[min(iz, p.nnz - 1)];
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int ix = s.x0 + xw + r;
-                ixr[r] = ix;
                 act[r] = zact && ix < p.nnx - MM;
-                fx[r] = p.fx[min(ix, p.nnx - 1)];
-                rec[r] = iz == p.gz && ix >= p.rx0 && ix < p.rx0 + p.nx;
+                const int cxi = min(ix, p.nnx - 1);
+                fx[r] = p.fx[cxi];
+                rec[r] = act[r] && iz == p.gz && ix >= p.rx0 && ix < p.rx0 + p.nx;
+                trb[r] = ix - p.rx0;
+                srow[r] = act[r] && ix == p.s_x;
+                gb[r] = (uint32_t)iz + (uint32_t)p.ldz * (uint32_t)cxi;
             }
         },
-        [&](unsigned char *st, const Seg &, int) {
-            const S *At = reinterpret_cast<const S *>(st);
+        [&](auto ph, uint32_t sa, const Seg &, int) {
+            constexpr int Q = decltype(ph)::value;
+            const S *At = reinterpret_cast<const S *>(ringA + sa * L::A_STRIDE);
 #pragma unroll
-            for (int r = 0; r < R; ++r) {
-#pragma unroll
-                for (int i = 0; i < 8; ++i) win[r][i] = win[r][i + 1];
-                win[r][8] = (T)At[(xw + r + MM) * L::AW + tz + MM];
-            }
+            for (int r = 0; r < R; ++r) win[r][Q] = (T)At[c0 + r * AW];
         },
-        [&](unsigned char *sa, unsigned char *sb, const Seg &, int o) {
-            if (!zact) return;
-            const S *Ao = reinterpret_cast<const S *>(sa);
-            const S *Bp = reinterpret_cast<const S *>(sb);
-            const float *Bv = reinterpret_cast<const float *>(sb + L::B_BYTES);
+        [&](int ph, uint32_t sa, uint32_t sh, uint32_t sb, const Seg &, int q) {
+            const int o = q - MM;
+            const S *At = reinterpret_cast<const S *>(ringA + sa * L::A_STRIDE);
+            // y part of the Laplacian from the window cur(o-4 .. o+3) (plane o+m in slot
+            // (ph+4+m)&7) and the fresh plane cur(o+4) = cur(q) (2O:288), which then
+            // replaces cur(q-8) in the window
+            T cur[R], c3[R];
+            with_phase(ph, [&](auto pc) {
+                constexpr int Q = decltype(pc)::value;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const T *wr = win[r];
+                    const T nw = (T)At[c0 + r * AW];
+                    const T cc = wr[(Q + 4) & 7];
+                    T a = (T)S8_0 * cc;
+                    a = fma_t(k1, wr[(Q + 5) & 7] + wr[(Q + 3) & 7], a);
+                    a = fma_t(k2, wr[(Q + 6) & 7] + wr[(Q + 2) & 7], a);
+                    a = fma_t(k3, wr[(Q + 7) & 7] + wr[(Q + 1) & 7], a);
+                    a = fma_t(k4, nw + wr[Q], a);
+                    cur[r] = cc;
+                    c3[r] = a;
+                    win[r][Q] = nw;
+                }
+            });
+            const S *Ao = reinterpret_cast<const S *>(ringA + sh * L::A_STRIDE);
+            const unsigned char *sbp = ringB + sb * L::B_STRIDE;
+            const S *Bp = reinterpret_cast<const S *>(sbp);
+            const float *Bv = reinterpret_cast<const float *>(sbp + L::B_BYTES);
             const float2 fy = p.fy[o];
             // current level at tile rows xw .. xw+R+7 of this z column: xs[j] = cur(x = xw - 4 + j)
             T xs[R + 8];
 #pragma unroll
-            for (int j = 0; j < R + 8; ++j) xs[j] = (T)Ao[(xw + j) * L::AW + tz + MM];
-            const size_t po = pstride * o;
+            for (int j = 0; j < R + 8; ++j) xs[j] = (T)Ao[c0 + (j - MM) * AW];
+            const uint32_t po = pstride * (uint32_t)o;
+            const bool yrec = o >= p.ry0 && o < p.ry0 + p.ny;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                if (!act[r]) continue;
-                const int c = (xw + r + MM) * L::AW + tz + MM, bi = (xw + r) * 32 + tz;
-                const T cur = win[r][4];
-                T c1 = (T)S8_0 * cur, c2 = c1, c3 = c1;
-                // z from the tile, x from the shared rows, y from the window (2O:284-289)
+                const int c = c0 + r * AW, bi = (xw + r) * 32 + tz;
+                T c1 = (T)S8_0 * cur[r], c2 = c1;
+                // z from the tile, x from the shared rows (2O:284-289)
                 c1 = fma_t(k1, (T)Ao[c - 1] + (T)Ao[c + 1], c1);
                 c2 = fma_t(k1, xs[r + 3] + xs[r + 5], c2);
-                c3 = fma_t(k1, win[r][5] + win[r][3], c3);
                 c1 = fma_t(k2, (T)Ao[c - 2] + (T)Ao[c + 2], c1);
                 c2 = fma_t(k2, xs[r + 2] + xs[r + 6], c2);
-                c3 = fma_t(k2, win[r][6] + win[r][2], c3);
                 c1 = fma_t(k3, (T)Ao[c - 3] + (T)Ao[c + 3], c1);
                 c2 = fma_t(k3, xs[r + 1] + xs[r + 7], c2);
-                c3 = fma_t(k3, win[r][7] + win[r][1], c3);
                 c1 = fma_t(k4, (T)Ao[c - 4] + (T)Ao[c + 4], c1);
                 c2 = fma_t(k4, xs[r] + xs[r + 8], c2);
-                c3 = fma_t(k4, win[r][8] + win[r][0], c3);
-                c1 *= (T)p.dz2;
-                c2 *= (T)p.dx2;
-                c3 *= (T)p.dy2;
-                const T m = (T)Bv[bi] * ((c1 + c2) + c3);
+                c1 *= dz2;
+                c2 *= dx2;
+                const T m = (T)Bv[bi] * ((c1 + c2) + c3[r] * dy2);
                 const T prev = sponge3<T>((T)Bp[bi], fy, fx[r], fz);
                 T nxt;
                 if constexpr (sizeof(T) == 4)
-                    nxt = upd2o(cur, prev, m);
+                    nxt = upd2o(cur[r], prev, m);
                 else
-                    nxt = (T(2) * cur - prev) + m;
+                    nxt = (T(2) * cur[r] - prev) + m;
                 nxt = sponge3<T>(nxt, fy, fx[r], fz);
-                if (ixr[r] == p.s_x && o == p.s_y) {  // next step's dipole (2O:184-185)
+                if (srow[r] && o == p.s_y) {  // next step's dipole (2O:184-185)
                     if (iz == p.s_z) nxt = nxt + (T)p.w_next;
                     if (iz == p.s_z + 2) nxt = nxt - (T)p.w_next;
                 }
-                ybuf[(size_t)iz + (size_t)p.ldz * ixr[r] + po] = to_store<S, T>(nxt);
-                if (rec[r] && o >= p.ry0 && o < p.ry0 + p.ny) {  // cuda_record after absorb (2O:452)
-                    const size_t tr = (size_t)(ixr[r] - p.rx0) + (size_t)p.nx * (o - p.ry0);
-                    T rr = sponge3<T>(cur, fy, fx[r], fz);
+                if (act[r]) ybuf[gb[r] + po] = to_store<S, T>(nxt);
+                if (rec[r] && yrec) {  // cuda_record after absorb (2O:452)
+                    const size_t tr = (size_t)trb[r] + (size_t)p.nx * (o - p.ry0);
+                    T rr = sponge3<T>(cur[r], fy, fx[r], fz);
                     if (p.mute_nt && p.it < p.mute_nt[tr]) rr = T(0);
                     p.rec[tr * p.nt + p.it] = (float)rr;
                 }

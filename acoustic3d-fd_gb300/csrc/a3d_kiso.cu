@@ -11,6 +11,8 @@
 // Each consumer warp owns R consecutive x rows of the 32 x TX tile (lane = z), so
 // the per-plane pipeline work is shared by R cells and the x-derivative reads
 // R + 7 tile rows instead of 8 R.
+#include <climits>
+
 #include "a3d_k1dev.cuh"
 
 namespace a3d {
@@ -27,7 +29,7 @@ struct IsoVelL {
     static constexpr size_t A_STRIDE = (A_BYTES + 127) / 128 * 128;
     static constexpr size_t B_STRIDE = (B_BYTES + 127) / 128 * 128;
     static constexpr size_t BAR_OFF = KA * A_STRIDE + KB * B_STRIDE;
-    static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBars<KA, KB>);
+    static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBarsM<KA, KB>);
 };
 
 template <int TX, class S, int D, int R>
@@ -36,9 +38,9 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
             S *__restrict__ w, const __grid_constant__ K1Params p) {
     using L = IsoVelL<TX, S, D>;
     using T = typename Arith<S>::T;
-    constexpr int NW = TX / R, NC = 32 * NW;
+    constexpr int NW = TX / R, NC = 32 * NW, AW = L::AW;
     extern __shared__ __align__(128) unsigned char smem[];
-    auto &bars = *reinterpret_cast<PipeBars<L::KA, L::KB> *>(smem + L::BAR_OFF);
+    auto &bars = *reinterpret_cast<PipeBarsM<L::KA, L::KB> *>(smem + L::BAR_OFF);
     unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
     if (threadIdx.x == 0) bars.init(NW);
     __syncthreads();
@@ -50,13 +52,13 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
     if (warp == NW) {
         if (lane != 0) return;
         for (int i = 0; i < 5; ++i) prefetch_tmap(&mp.m[i]);
-        pipe_produce<TX, L::KA, L::KB>(
-            p.sw, w0, w1, bars, ringA, L::A_STRIDE, L::A_BYTES, ringB, L::B_STRIDE, L::B_BYTES,
-            p.err,
-            [&](unsigned char *dst, uint64_t *bar, const Seg &s, int q) {
-                tma_load_3d(dst, &mp.m[0], bar, s.z0 - MM, s.x0 - MM, q);
-            },
-            [&](unsigned char *dst, uint64_t *bar, const Seg &s, int o) {
+        pipe_produce_m<TX, L::KA, L::KB>(
+            p.sw, w0, w1, bars, p.err, [&](uint32_t sa, int sb, uint64_t *bar, const Seg &s, int q) {
+                mbar_arrive_expect_tx(bar, L::A_BYTES + (sb >= 0 ? L::B_BYTES : 0u));
+                tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0 - MM, s.x0 - MM, q);
+                if (sb < 0) return;
+                unsigned char *dst = ringB + sb * L::B_STRIDE;
+                const int o = q - MM;
                 tma_load_3d(dst, &mp.m[1], bar, s.z0, s.x0, o);
                 tma_load_3d(dst + L::C * sizeof(S), &mp.m[2], bar, s.z0, s.x0, o);
                 tma_load_3d(dst + 2 * L::C * sizeof(S), &mp.m[3], bar, s.z0, s.x0, o);
@@ -66,85 +68,106 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
     }
 
     const int tz = lane, xw = warp * R;  // this warp's first tile row
-    T win[R][9];
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-#pragma unroll
-        for (int i = 0; i < 9; ++i) win[r][i] = T(0);
-    int iz = 0;
-    bool zact = false, act[R];
-    T cx1[R], cx2[R], cz1 = 0, cz2 = 0;
-    size_t gb[R];  // this column's row offsets in the fields
-    const size_t pstride = (size_t)p.ldz * p.nnx;
-    pipe_consume<TX, L::KA, L::KB>(
-        p.sw, w0, w1, bars, ringA, L::A_STRIDE, ringB, L::B_STRIDE, p.err,
+    const int c0 = (xw + MM) * AW + tz + MM;  // this thread's first cell in an A tile
+    T win[R][8];                              // P at the last 8 planes, slot = item mod 8
+    bool act[R];
+    T cx1d[R], cx2[R], cz1d = 0, cz2 = 0;
+    uint32_t gb[R];  // in-plane offsets of this thread's cells
+    int srcq = INT_MIN;
+    const uint32_t pstride = (uint32_t)p.ldz * (uint32_t)p.nnx;
+    const T k[4] = {(T)C8_0, (T)C8_1, (T)C8_2, (T)C8_3};
+    // the dipole enters the sweep's view of P (..iso..:94): patch the A tile of the
+    // source plane in place (it serves the window push and, 4 planes later, the
+    // in-plane neighbours), then make the write visible to every consumer warp
+    auto inject = [&](S *A, const Seg &s) {
+        const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - MM);
+        if (threadIdx.x == 0) {
+            if (lz >= 0 && lz < AW) A[lx * AW + lz] = to_store<S, T>(ld<T>(A, lx * AW + lz) + (T)p.amp0);
+            if (lz + 2 >= 0 && lz + 2 < AW)
+                A[lx * AW + lz + 2] = to_store<S, T>(ld<T>(A, lx * AW + lz + 2) + (T)p.amp1);
+            fence_proxy_async();  // the stage is refilled by TMA later
+        }
+        consumer_sync(NC);
+    };
+    pipe_run<TX, L::KA, L::KB, MM>(
+        p.sw, w0, w1, bars, p.err,
         [&](const Seg &s) {
-            iz = s.z0 + tz;
-            zact = iz < p.nnz - MM;
+            const int iz = s.z0 + tz;
+            const bool zact = iz < p.nnz - MM;
             const int cz = min(iz, p.nnz - 1);
-            cz1 = (T)p.cz1[cz];
+            cz1d = (T)p.cz1[cz] * (T)p.dtz;
             cz2 = (T)p.cz2[cz];
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int ix = s.x0 + xw + r;
                 act[r] = zact && ix < p.nnx - MM;
                 const int cxi = min(ix, p.nnx - 1);
-                cx1[r] = (T)p.cx1[cxi];
+                cx1d[r] = (T)p.cx1[cxi] * (T)p.dtx;
                 cx2[r] = (T)p.cx2[cxi];
-                gb[r] = (size_t)iz + (size_t)p.ldz * cxi;
+                gb[r] = (uint32_t)iz + (uint32_t)p.ldz * (uint32_t)cxi;
             }
+            const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - MM);
+            srcq = (p.inj && lx >= 0 && lx < L::AH && lz + 2 >= 0 && lz < AW) ? p.s_y : INT_MIN;
         },
-        [&](unsigned char *st, const Seg &s, int q) {
-            S *A = reinterpret_cast<S *>(st);
-            if (p.inj && q == p.s_y) {  // the dipole enters the view of P, ..iso..:94
-                const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - MM);
-                if (threadIdx.x == 0 && lx >= 0 && lx < L::AH) {
-                    if (lz >= 0 && lz < L::AW)
-                        A[lx * L::AW + lz] = to_store<S, T>(ld<T>(A, lx * L::AW + lz) + (T)p.amp0);
-                    if (lz + 2 >= 0 && lz + 2 < L::AW)
-                        A[lx * L::AW + lz + 2] = to_store<S, T>(ld<T>(A, lx * L::AW + lz + 2) + (T)p.amp1);
+        [&](auto ph, uint32_t sa, const Seg &s, int q) {
+            constexpr int P = decltype(ph)::value;
+            S *A = reinterpret_cast<S *>(ringA + sa * L::A_STRIDE);
+            if (q == srcq) inject(A, s);
+#pragma unroll
+            for (int r = 0; r < R; ++r) win[r][P] = ld<T>(A, c0 + r * AW);
+        },
+        [&](int ph, uint32_t sa, uint32_t sh, uint32_t sb, const Seg &s, int q) {
+            S *A = reinterpret_cast<S *>(ringA + sa * L::A_STRIDE);
+            if (q == srcq) inject(A, s);
+            // window push of P(q) and the y-derivative at o = q - 4 (..iso..:126)
+            T yy[R];
+            with_phase(ph, [&](auto pc) {
+                constexpr int P = decltype(pc)::value;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    win[r][P] = ld<T>(A, c0 + r * AW);
+                    T a = 0;
+#pragma unroll
+                    for (int im = 0; im < 4; ++im)  // P(o+1+m) in slot (P+5+m)&7, P(o-m) in (P+4-m)&7
+                        a = fma_t(k[im], win[r][(P + 5 + im) & 7] - win[r][(P + 4 - im) & 7], a);
+                    yy[r] = a;
                 }
-                consumer_sync(NC);
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-#pragma unroll
-                for (int i = 0; i < 8; ++i) win[r][i] = win[r][i + 1];
-                win[r][8] = ld<T>(A, (xw + r + MM) * L::AW + tz + MM);
-            }
-        },
-        [&](unsigned char *sa, unsigned char *sb, const Seg &, int o) {
-            if (!zact) return;
-            const S *A = reinterpret_cast<const S *>(sa);
-            const S *Bu = reinterpret_cast<const S *>(sb);
+            });
+            // output plane o = q - 4: its P tile is the A stage held since item q - 4
+            const int o = q - MM;
+            const S *Ao = reinterpret_cast<const S *>(ringA + sh * L::A_STRIDE);
+            const unsigned char *sbp = ringB + sb * L::B_STRIDE;
+            const S *Bu = reinterpret_cast<const S *>(sbp);
             const S *Bv = Bu + L::C, *Bw = Bu + 2 * L::C;
-            const float *Br = reinterpret_cast<const float *>(sb + 3 * L::C * sizeof(S));
-            const T k[4] = {(T)C8_0, (T)C8_1, (T)C8_2, (T)C8_3};
+            const float *Br = reinterpret_cast<const float *>(sbp + 3 * L::C * sizeof(S));
             // P at tile rows xw+1 .. xw+R+7 of this z column: xs[j] = P(x = xw - 3 + j)
             T xs[R + 7];
 #pragma unroll
-            for (int j = 0; j < R + 7; ++j) xs[j] = ld<T>(A, (xw + 1 + j) * L::AW + tz + MM);
-            const T cy1 = (T)p.cy1[o], cy2 = (T)p.cy2[o];
-            const size_t po = pstride * o;
+            for (int j = 0; j < R + 7; ++j) xs[j] = ld<T>(Ao, c0 + (j + 1 - MM) * AW);
+            const T cy1d = (T)p.cy1[o] * (T)p.dty, cy2 = (T)p.cy2[o];
+            const uint32_t po = pstride * (uint32_t)o;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                if (!act[r]) continue;
-                const int c = (xw + r + MM) * L::AW + tz + MM, bi = (xw + r) * 32 + tz;
-                T xx = 0, yy = 0, zz = 0;
+                const int c = c0 + r * AW, bi = (xw + r) * 32 + tz;
+                T xx = 0, zz = 0;
 #pragma unroll
                 for (int im = 0; im < 4; ++im) {  // ..iso..:125-127
-                    yy = fma_t(k[im], win[r][5 + im] - win[r][4 - im], yy);
                     xx = fma_t(k[im], xs[r + 4 + im] - xs[r + 3 - im], xx);
-                    zz = fma_t(k[im], ld<T>(A, c + im + 1) - ld<T>(A, c - im), zz);
+                    zz = fma_t(k[im], ld<T>(Ao, c + im + 1) - ld<T>(Ao, c - im), zz);
                 }
                 const T ri = (T)Br[bi];  // 1/rho
                 xx = xx * ri;
-                yy = yy * ri;
+                const T yr = yy[r] * ri;
                 zz = zz * ri;
-                const size_t g = gb[r] + po;
-                u[g] = to_store<S, T>(fma_t(cx2[r], ld<T>(Bu, bi), -((cx1[r] * (T)p.dtx) * xx)));
-                v[g] = to_store<S, T>(fma_t(cy2, ld<T>(Bv, bi), -((cy1 * (T)p.dty) * yy)));
-                w[g] = to_store<S, T>(fma_t(cz2, ld<T>(Bw, bi), -((cz1 * (T)p.dtz) * zz)));
+                const T un = fma_t(cx2[r], ld<T>(Bu, bi), -(cx1d[r] * xx));
+                const T vn = fma_t(cy2, ld<T>(Bv, bi), -(cy1d * yr));
+                const T wn = fma_t(cz2, ld<T>(Bw, bi), -(cz1d * zz));
+                if (act[r]) {
+                    const uint32_t g = gb[r] + po;
+                    u[g] = to_store<S, T>(un);
+                    v[g] = to_store<S, T>(vn);
+                    w[g] = to_store<S, T>(wn);
+                }
             }
         });
 }
@@ -163,7 +186,7 @@ struct IsoStrL {
     static constexpr size_t A_STRIDE = (A_BYTES + 127) / 128 * 128;
     static constexpr size_t B_STRIDE = (B_BYTES + 127) / 128 * 128;
     static constexpr size_t BAR_OFF = KA * A_STRIDE + KB * B_STRIDE;
-    static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBars<KA, KB>);
+    static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBarsM<KA, KB>);
 };
 
 template <int TX, class S, int D, int R>
@@ -174,7 +197,7 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
     using T = typename Arith<S>::T;
     constexpr int NW = TX / R;
     extern __shared__ __align__(128) unsigned char smem[];
-    auto &bars = *reinterpret_cast<PipeBars<L::KA, L::KB> *>(smem + L::BAR_OFF);
+    auto &bars = *reinterpret_cast<PipeBarsM<L::KA, L::KB> *>(smem + L::BAR_OFF);
     unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
     if (threadIdx.x == 0) bars.init(NW);
     __syncthreads();
@@ -190,16 +213,20 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
     if (warp == NW) {
         if (lane != 0) return;
         for (int i = 0; i < 9; ++i) prefetch_tmap(&mp.m[i]);
-        pipe_produce<TX, L::KA, L::KB>(
-            p.sw, w0, w1, bars, ringA, L::A_STRIDE, L::A_BYTES, ringB, L::B_STRIDE, 0, p.err,
-            [&](unsigned char *dst, uint64_t *bar, const Seg &s, int q) {
-                tma_load_3d(dst, &mp.m[0], bar, s.z0, s.x0, q);
-            },
-            [&](unsigned char *dst, uint64_t *bar, const Seg &s, int o) {
+        pipe_produce_m<TX, L::KA, L::KB>(
+            p.sw, w0, w1, bars, p.err, [&](uint32_t sa, int sb, uint64_t *bar, const Seg &s, int q) {
+                if (sb < 0) {
+                    mbar_arrive_expect_tx(bar, L::A_BYTES);
+                    tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0, s.x0, q);
+                    return;
+                }
+                const int o = q - MM;
                 const bool nx_ = range_damped(s.x0, TX, p.ulo[0], p.uhi[0]);
                 const bool ny_ = range_damped(o, 1, p.ulo[1], p.uhi[1]);
                 const bool nz_ = range_damped(s.z0, 32, p.ulo[2], p.uhi[2]);
-                mbar_arrive_expect_tx(bar, L::B_FIXED + AUX * ((int)nx_ + (int)ny_ + (int)nz_));
+                mbar_arrive_expect_tx(bar, L::A_BYTES + L::B_FIXED + AUX * ((int)nx_ + (int)ny_ + (int)nz_));
+                tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0, s.x0, q);
+                unsigned char *dst = ringB + sb * L::B_STRIDE;
                 tma_load_3d(dst, &mp.m[1], bar, s.z0, s.x0 - MM, o);
                 tma_load_3d(dst + oW, &mp.m[2], bar, s.z0 - MM, s.x0, o);
                 tma_load_3d(dst + oP, &mp.m[3], bar, s.z0, s.x0, o);
@@ -213,23 +240,23 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
     }
 
     const int tz = lane, xw = warp * R;
-    T win[R][9];
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-#pragma unroll
-        for (int i = 0; i < 9; ++i) win[r][i] = T(0);
-    int iz = 0;
-    bool zact = false, dzm = false, act[R], dxm[R], rec[R];
+    T win[R][8];  // v at the last 8 planes, slot = item mod 8
+    bool dzm = false, act[R], dxm[R], rec[R];
     float ax1[R], ax2[R], az1 = 1, az2 = 1;
-    int ixr[R];
+    uint32_t gb[R];
+    int trb[R];  // receiver trace index of this cell at y = npml, or -1
+    bool fast = false;  // tile undamped in x and z, every cell active, no receivers
+    uint32_t g0 = 0;    // in-plane offset of this thread's first cell
     S *px = reinterpret_cast<S *>(p.px), *py = reinterpret_cast<S *>(p.py),
       *pz = reinterpret_cast<S *>(p.pz);
-    const size_t pstride = (size_t)p.ldz * p.nnx;
-    pipe_consume<TX, L::KA, L::KB>(
-        p.sw, w0, w1, bars, ringA, L::A_STRIDE, ringB, L::B_STRIDE, p.err,
+    const uint32_t pstride = (uint32_t)p.ldz * (uint32_t)p.nnx;
+    const T k[4] = {(T)C8_0, (T)C8_1, (T)C8_2, (T)C8_3};
+    const T dtx = (T)p.dtx, dty = (T)p.dty, dtz = (T)p.dtz;
+    pipe_run<TX, L::KA, L::KB, 0>(
+        p.sw, w0, w1, bars, p.err,
         [&](const Seg &s) {
-            iz = s.z0 + tz;
-            zact = iz < p.nnz - MM;
+            const int iz = s.z0 + tz;
+            const bool zact = iz < p.nnz - MM;
             const int cz = min(iz, p.nnz - 1);
             az1 = p.az1[cz];
             az2 = p.az2[cz];
@@ -238,67 +265,117 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int ix = s.x0 + xw + r;
-                ixr[r] = ix;
                 act[r] = zact && ix < p.nnx - MM;
                 const int cxi = min(ix, p.nnx - 1);
                 ax1[r] = p.ax1[cxi];
                 ax2[r] = p.ax2[cxi];
                 dxm[r] = damped(ax1[r], ax2[r]);
-                rec[r] = rec_z && ix >= p.npml && ix < p.npml + p.nx;
+                rec[r] = act[r] && rec_z && ix >= p.npml && ix < p.npml + p.nx;
+                trb[r] = ix - p.npml;
+                gb[r] = (uint32_t)iz + (uint32_t)p.ldz * (uint32_t)cxi;
             }
+            g0 = gb[0];
+            fast = !range_damped(s.x0, TX, p.ulo[0], p.uhi[0]) && !range_damped(s.z0, 32, p.ulo[2], p.uhi[2]) &&
+                   !(p.npml >= s.z0 && p.npml < s.z0 + 32);
         },
-        [&](unsigned char *st, const Seg &, int) {
-            const S *A = reinterpret_cast<const S *>(st);
+        [&](auto ph, uint32_t sa, const Seg &, int) {
+            constexpr int Q = decltype(ph)::value;
+            const S *A = reinterpret_cast<const S *>(ringA + sa * L::A_STRIDE);
 #pragma unroll
-            for (int r = 0; r < R; ++r) {
-#pragma unroll
-                for (int i = 0; i < 8; ++i) win[r][i] = win[r][i + 1];
-                win[r][8] = ld<T>(A, (xw + r) * 32 + tz);
-            }
+            for (int r = 0; r < R; ++r) win[r][Q] = ld<T>(A, (xw + r) * 32 + tz);
         },
-        [&](unsigned char *, unsigned char *sb, const Seg &, int o) {
-            if (!zact) return;
-            const S *Bu = reinterpret_cast<const S *>(sb);
-            const S *Bw = reinterpret_cast<const S *>(sb + oW);
-            const S *Bp = reinterpret_cast<const S *>(sb + oP);
-            const float *Br = reinterpret_cast<const float *>(sb + oR);
-            const float *Bvp = reinterpret_cast<const float *>(sb + oV);
-            const S *Bx = reinterpret_cast<const S *>(sb + oX);
+        [&](int ph, uint32_t sa, uint32_t, uint32_t sb, const Seg &, int q) {
+            const int o = q - MM;
+            // y-derivative at o from the window v(o-4 .. o+3) (plane o+m in slot
+            // (ph+4+m)&7; ..iso..:179), then v(q) replaces v(q-8), which it last served
+            const S *A = reinterpret_cast<const S *>(ringA + sa * L::A_STRIDE);
+            T yy[R];
+            with_phase(ph, [&](auto pc) {
+                constexpr int Q = decltype(pc)::value;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    T a = 0;
+#pragma unroll
+                    for (int im = 0; im < 4; ++im)
+                        a = fma_t(k[im], win[r][(Q + 4 + im) & 7] - win[r][(Q + 3 - im) & 7], a);
+                    yy[r] = a;
+                    win[r][Q] = ld<T>(A, (xw + r) * 32 + tz);
+                }
+            });
+            const unsigned char *sbp = ringB + sb * L::B_STRIDE;
+            const S *Bu = reinterpret_cast<const S *>(sbp);
+            const S *Bw = reinterpret_cast<const S *>(sbp + oW);
+            const S *Bp = reinterpret_cast<const S *>(sbp + oP);
+            const float *Br = reinterpret_cast<const float *>(sbp + oR);
+            const float *Bvp = reinterpret_cast<const float *>(sbp + oV);
+            const S *Bx = reinterpret_cast<const S *>(sbp + oX);
             const S *By = Bx + L::C, *Bz = Bx + 2 * L::C;
-            const T k[4] = {(T)C8_0, (T)C8_1, (T)C8_2, (T)C8_3};
             // u at tile rows xw .. xw+R+6 of this z column: us[j] = u(x = xw - 4 + j)
             T us[R + 7];
 #pragma unroll
             for (int j = 0; j < R + 7; ++j) us[j] = ld<T>(Bu, (xw + j) * 32 + tz);
+            const bool dym = o < p.ulo[1] || o >= p.uhi[1];  // == damped(ay1[o], ay2[o])
+            const uint32_t po = pstride * (uint32_t)o;
+            if (fast && !dym) {  // undamped interior tile and plane: P - gx - gy - gz, a1 == 1
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int bi = (xw + r) * 32 + tz, cw = (xw + r) * 40 + tz + MM;
+                    T xx = 0, zz = 0;
+#pragma unroll
+                    for (int im = 0; im < 4; ++im) {  // ..iso..:178-180
+                        xx = fma_t(k[im], us[r + 4 + im] - us[r + 3 - im], xx);
+                        zz = fma_t(k[im], ld<T>(Bw, cw + im) - ld<T>(Bw, cw - im - 1), zz);
+                    }
+                    // (((1 * rho) * vp) * vp) == (rho * vp) * vp  (..iso..:182-184)
+                    const T t = ((T)Br[bi] * (T)Bvp[bi]) * (T)Bvp[bi];
+                    const T gx = (t * dtx) * xx, gy = (t * dty) * yy[r], gz = (t * dtz) * zz;
+                    P[g0 + (uint32_t)(r * p.ldz) + po] = to_store<S, T>(((ld<T>(Bp, bi) - gx) - gy) - gz);
+                }
+                return;
+            }
             const float ay1 = p.ay1[o], ay2 = p.ay2[o];
-            const bool dym = damped(ay1, ay2);
-            const size_t po = pstride * o;
+            const bool yrec = o >= p.npml && o < p.npml + p.ny;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                if (!act[r]) continue;
                 const int bi = (xw + r) * 32 + tz, cw = (xw + r) * 40 + tz + MM;
-                T xx = 0, yy = 0, zz = 0;
+                T xx = 0, zz = 0;
 #pragma unroll
                 for (int im = 0; im < 4; ++im) {  // ..iso..:178-180
-                    yy = fma_t(k[im], win[r][4 + im] - win[r][3 - im], yy);
                     xx = fma_t(k[im], us[r + 4 + im] - us[r + 3 - im], xx);
                     zz = fma_t(k[im], ld<T>(Bw, cw + im) - ld<T>(Bw, cw - im - 1), zz);
                 }
+                const T yr = yy[r];
                 const T rv = (T)Br[bi], vv = (T)Bvp[bi];
-                const T gx = (((((T)ax1[r] * rv) * vv) * vv) * (T)p.dtx) * xx;  // ..iso..:182-184
-                const T gy = (((((T)ay1 * rv) * vv) * vv) * (T)p.dty) * yy;
-                const T gz = (((((T)az1 * rv) * vv) * vv) * (T)p.dtz) * zz;
-                const size_t g = (size_t)iz + (size_t)p.ldz * ixr[r] + po;
-                T cx = dxm[r] ? ld<T>(Bx, bi) : T(0), cy = dym ? ld<T>(By, bi) : T(0),
-                  cz = dzm ? ld<T>(Bz, bi) : T(0);
-                const T Pn = pupdate_r<T>(ld<T>(Bp, bi), gx, gy, gz, dxm[r], dym, dzm, ax2[r], ay2, az2,
-                                          cx, cy, cz);
-                P[g] = to_store<S, T>(Pn);
-                if (dxm[r]) px[g] = to_store<S, T>(cx);
-                if (dym) py[g] = to_store<S, T>(cy);
-                if (dzm) pz[g] = to_store<S, T>(cz);
-                if (rec[r] && o >= p.npml && o < p.npml + p.ny) {  // ..iso..:294-304
-                    const size_t tr = (size_t)(ixr[r] - p.npml) + (size_t)p.nx * (o - p.npml);
+                T gx, gy, gz;
+                const bool dmp = dxm[r] | dym | dzm;
+                if (!dmp) {  // a1 == 1 on every axis: (((1 * rho) * vp) * vp) == (rho * vp) * vp
+                    const T t = (rv * vv) * vv;
+                    gx = (t * dtx) * xx;
+                    gy = (t * dty) * yr;
+                    gz = (t * dtz) * zz;
+                } else {  // ..iso..:182-184
+                    gx = (((((T)ax1[r] * rv) * vv) * vv) * dtx) * xx;
+                    gy = (((((T)ay1 * rv) * vv) * vv) * dty) * yr;
+                    gz = (((((T)az1 * rv) * vv) * vv) * dtz) * zz;
+                }
+                const T Po = ld<T>(Bp, bi);
+                const uint32_t g = gb[r] + po;
+                T Pn;
+                if (!dmp) {
+                    Pn = ((Po - gx) - gy) - gz;
+                } else {
+                    T cx = dxm[r] ? ld<T>(Bx, bi) : T(0), cy = dym ? ld<T>(By, bi) : T(0),
+                      cz = dzm ? ld<T>(Bz, bi) : T(0);
+                    Pn = pupdate_r<T>(Po, gx, gy, gz, dxm[r], dym, dzm, ax2[r], ay2, az2, cx, cy, cz);
+                    if (act[r]) {
+                        if (dxm[r]) px[g] = to_store<S, T>(cx);
+                        if (dym) py[g] = to_store<S, T>(cy);
+                        if (dzm) pz[g] = to_store<S, T>(cz);
+                    }
+                }
+                if (act[r]) P[g] = to_store<S, T>(Pn);
+                if (rec[r] && yrec) {  // ..iso..:294-304
+                    const size_t tr = (size_t)trb[r] + (size_t)p.nx * (o - p.npml);
                     T rr = Pn;
                     if (p.mute_nt && p.it < p.mute_nt[tr]) rr = T(0);
                     p.rec[tr * p.nt + p.it] = (float)rr;

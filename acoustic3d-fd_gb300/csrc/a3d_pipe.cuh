@@ -18,6 +18,8 @@
 // CTA-wide abort flag so the other role stops, and the producer drains all
 // copies it issued before the CTA exits.
 #pragma once
+#include <type_traits>
+
 #include "a3d_common.cuh"
 
 namespace a3d {
@@ -101,10 +103,11 @@ __device__ __forceinline__ void pipe_produce(const Sweep &sw, long long w0, long
         w = wend;
     }
     // drain: every issued copy must land before the CTA's shared memory goes away
+    // (also after an abort: only the time limit ends these waits)
     for (uint32_t j = (ja > KA ? ja - KA : 0); j < ja; ++j)
-        if (!mbar_wait(&b.fullA[j % KA], (j / KA) & 1, err, KERR_DRAIN_TIMEOUT, ab)) break;
+        if (!mbar_wait(&b.fullA[j % KA], (j / KA) & 1, err, KERR_DRAIN_TIMEOUT, nullptr)) break;
     for (uint32_t j = (jb > KB ? jb - KB : 0); j < jb; ++j)
-        if (!mbar_wait(&b.fullB[j % KB], (j / KB) & 1, err, KERR_DRAIN_TIMEOUT, ab)) break;
+        if (!mbar_wait(&b.fullB[j % KB], (j / KB) & 1, err, KERR_DRAIN_TIMEOUT, nullptr)) break;
 }
 
 // Consumers: all consumer threads.  onSeg(seg) at a segment start; onLoad(stageA, seg, q)
@@ -137,6 +140,140 @@ __device__ __forceinline__ bool pipe_consume(const Sweep &sw, long long w0, long
             __syncwarp();
             if (ja >= MM && (threadIdx.x & 31) == 0) mbar_arrive(&b.emptyA[(ja - MM) % KA]);
             ++ja;
+        }
+        w = wend;
+    }
+    return true;
+}
+
+// ===========================================================================
+// Merged-item pipeline with a phase-unrolled consumer.
+//
+// Item j of a segment (plane q = ya-4+j) carries the A copy of plane q and, from
+// q = ya+4 on, the B copies of output plane o = q-4; all of them complete on
+// full[j % KA], so a consumer waits once per plane.  A stages are released HOLD
+// items after their arrival (HOLD = 4 when the output step reads the in-plane
+// neighbours of A at plane o, 0 when only the y-window reads A), B stages right
+// after the output step.  An 8-plane register window rotates by renaming: plane
+// q sits in slot (item index mod 8), and the window code is dispatched on that
+// phase (with_phase), so no register moves shift the window.
+namespace detail {
+template <int I, int N, class F>
+__device__ __forceinline__ void static_for(F &&f) {
+    if constexpr (I < N) {
+        f(std::integral_constant<int, I>{});
+        static_for<I + 1, N>(f);
+    }
+}
+}  // namespace detail
+
+template <int KA, int KB>
+struct PipeBarsM {
+    uint64_t full[KA], emptyA[KA], emptyB[KB];
+    int abort_flag;
+    __device__ void init(int nconsumers) {  // nconsumers: consumer warps
+        for (int i = 0; i < KA; ++i) { mbar_init(&full[i], 1); mbar_init(&emptyA[i], nconsumers); }
+        for (int i = 0; i < KB; ++i) mbar_init(&emptyB[i], nconsumers);
+        abort_flag = 0;
+        fence_mbar_init();
+    }
+    __device__ volatile int *abort_ptr() { return &abort_flag; }
+};
+
+// Producer (one thread): issue(sa, sb, bar, seg, q) posts the item's expect_tx on
+// bar and issues its copies: the A copy of plane q into A stage sa and, when
+// sb >= 0, the B copies of plane q-4 into B stage sb.
+template <int TX, int KA, int KB, class Issue>
+__device__ __forceinline__ void pipe_produce_m(const Sweep &sw, long long w0, long long w1,
+                                               PipeBarsM<KA, KB> &b, int *err, Issue issue) {
+    static_assert((KA & (KA - 1)) == 0 && (KB & (KB - 1)) == 0, "ring sizes are powers of two");
+    volatile int *ab = b.abort_ptr();
+    uint32_t ja = 0, jb = 0;
+    bool ok = true;
+    for (long long w = w0; w < w1 && ok;) {
+        long long wend;
+        const Seg s = make_seg<TX>(sw, w, w1, wend);
+        for (int q = s.ya - MM; q < s.yb + MM; ++q) {
+            const uint32_t sa = ja % KA;
+            if (ja >= KA && !(ok = mbar_wait(&b.emptyA[sa], ((ja / KA) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab)))
+                break;
+            int sb = -1;
+            if (q - MM >= s.ya) {
+                sb = (int)(jb % KB);
+                if (jb >= KB &&
+                    !(ok = mbar_wait(&b.emptyB[sb], ((jb / KB) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab)))
+                    break;
+                ++jb;
+            }
+            issue(sa, sb, &b.full[sa], s, q);
+            ++ja;
+        }
+        w = wend;
+    }
+    // drain (also after an abort): every issued copy lands on a full barrier
+    for (uint32_t j = (ja > KA ? ja - KA : 0); j < ja; ++j)
+        if (!mbar_wait(&b.full[j % KA], (j / KA) & 1, err, KERR_DRAIN_TIMEOUT, nullptr)) break;
+}
+
+// Phase dispatch: f(std::integral_constant<int, ph & 7>) through an 8-way switch, so
+// only the code that touches a rotating register window is replicated per phase.
+template <class F>
+__device__ __forceinline__ void with_phase(int ph, F &&f) {
+    switch (ph & 7) {
+    case 0: f(std::integral_constant<int, 0>{}); break;
+    case 1: f(std::integral_constant<int, 1>{}); break;
+    case 2: f(std::integral_constant<int, 2>{}); break;
+    case 3: f(std::integral_constant<int, 3>{}); break;
+    case 4: f(std::integral_constant<int, 4>{}); break;
+    case 5: f(std::integral_constant<int, 5>{}); break;
+    case 6: f(std::integral_constant<int, 6>{}); break;
+    default: f(std::integral_constant<int, 7>{}); break;
+    }
+}
+
+// Consumers (all consumer threads):
+//   onSeg(seg)                         at a segment start
+//   fill(ph, sa, seg, q)               planes q = ya-4 .. ya+3 (window fill); ph = item
+//                                      index in the segment (= q - ya + 4), a constant
+//   step(ph, sa, sh, sb, seg, q)       planes q >= ya+4: A stage sa (plane q), A stage sh
+//                                      (plane q-HOLD), B stage sb (output plane q-4);
+//                                      ph = item index mod 8 (run time: see with_phase)
+// Returns false on abort.
+template <int TX, int KA, int KB, int HOLD, class OnSeg, class Fill, class Step>
+__device__ __forceinline__ bool pipe_run(const Sweep &sw, long long w0, long long w1,
+                                         PipeBarsM<KA, KB> &b, int *err, OnSeg onSeg, Fill fill,
+                                         Step step) {
+    static_assert(HOLD == 0 || HOLD == MM, "A stages are held 0 or 4 items");
+    volatile int *ab = b.abort_ptr();
+    const bool lead = (threadIdx.x & 31) == 0;
+    uint32_t ja = 0, jb = 0;
+    bool ok = true;
+    for (long long w = w0; w < w1;) {
+        long long wend;
+        const Seg s = make_seg<TX>(sw, w, w1, wend);
+        onSeg(s);
+        detail::static_for<0, 8>([&](auto ph) {
+            if (!ok) return;
+            const uint32_t sa = ja % KA;
+            if (!(ok = mbar_wait(&b.full[sa], (ja / KA) & 1, err, KERR_FULL_TIMEOUT, ab))) return;
+            fill(ph, sa, s, s.ya - MM + decltype(ph)::value);
+            __syncwarp();
+            if (lead && ja >= HOLD) mbar_arrive(&b.emptyA[(ja - HOLD) % KA]);
+            ++ja;
+        });
+        if (!ok) return false;
+        const int qe = s.yb + MM;
+        for (int q = s.ya + MM; q < qe; ++q) {
+            const uint32_t sa = ja % KA, sh = (ja - HOLD) % KA, sb = jb % KB;
+            if (!mbar_wait(&b.full[sa], (ja / KA) & 1, err, KERR_FULL_TIMEOUT, ab)) return false;
+            step(q - s.ya + MM, sa, sh, sb, s, q);
+            __syncwarp();
+            if (lead) {
+                mbar_arrive(&b.emptyB[sb]);
+                mbar_arrive(&b.emptyA[sh]);
+            }
+            ++ja;
+            ++jb;
         }
         w = wend;
     }
