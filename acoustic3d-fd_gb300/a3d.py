@@ -39,6 +39,22 @@ class ShotPos(ctypes.Structure):
     _fields_ = [("sx", ctypes.c_int), ("sy", ctypes.c_int), ("sz", ctypes.c_int)]
 
 
+class Window(ctypes.Structure):
+    _fields_ = [("x0", ctypes.c_int), ("y0", ctypes.c_int), ("z0", ctypes.c_int),
+                ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int)]
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [("cfg", Config)] + [(n, ctypes.POINTER(ctypes.c_float)) for n in
+                                     ("vel", "rho", "eps", "del_", "theta", "phi")]
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("windows", ctypes.POINTER(Window)), ("graph", ctypes.c_int),
+                ("recs_host", ctypes.POINTER(ctypes.c_float)), ("rec_offsets", ctypes.POINTER(ctypes.c_size_t)),
+                ("ms", ctypes.POINTER(ctypes.c_double))]
+
+
 class A3DError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"acoustic3d status {code}: {msg}")
@@ -79,6 +95,9 @@ def lib() -> ctypes.CDLL:
         L.a3d_engine_kernel_times.restype = ctypes.c_int
         L.a3d_engine_describe.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
         L.a3d_engine_describe.restype = ctypes.c_int
+        L.a3d_run_batch.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(ShotPos), ctypes.c_int,
+                                    ctypes.POINTER(Opts)]
+        L.a3d_run_batch.restype = ctypes.c_int
         L.a3d_last_error.argtypes = []
         L.a3d_last_error.restype = ctypes.c_char_p
         _lib = L
@@ -205,3 +224,44 @@ def forward_host(cfg: Config, models: dict, shots, device: int = 0):
     recs = np.zeros((len(shots), cfg.ny, cfg.nx, cfg.nt), np.float32)
     _check(lib().a3d_forward_host(ctypes.byref(cfg), *ptrs, arr, len(shots), _fptr(recs), device))
     return recs
+
+
+def run_batch(cfg: Config, models: dict, shots, windows=None, graph: bool = False, device: int = 0):
+    """Every shot of a survey in one call (a3d_run_batch).
+
+    windows: None, or one (x0, y0, z0, nx, ny, nz) per shot (nx == 0: whole model).
+    Returns (records, ms): records[i] is shot i's [wny][wnx][nt] array, ms[i] the
+    device time of its time loop."""
+    n = cfg.nx * cfg.ny * cfg.nz
+    keep, ptrs = [], []
+    for name in MODEL_NAMES:
+        a = models.get(name)
+        if a is not None and name in READS[cfg.physics]:
+            a = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+            if a.size != n:
+                raise ValueError(f"model {name} has {a.size} values, expected {n}")
+            keep.append(a)
+            ptrs.append(_fptr(a))
+        else:
+            ptrs.append(_fptr(None))
+    pb = Problem(cfg, *ptrs)
+    ns = len(shots)
+    arr = (ShotPos * max(ns, 1))(*[ShotPos(*s) for s in shots])
+    dims = []
+    win = None
+    if windows is not None:
+        if len(windows) != ns:
+            raise ValueError("one window per shot")
+        win = (Window * max(ns, 1))(*[Window(*w) for w in windows])
+        dims = [(w[4], w[3]) if w[3] else (cfg.ny, cfg.nx) for w in windows]
+    else:
+        dims = [(cfg.ny, cfg.nx)] * ns
+    total = sum(a * b for a, b in dims) * cfg.nt
+    recs = np.zeros(max(total, 1), np.float32)
+    offs = (ctypes.c_size_t * max(ns, 1))()
+    ms = (ctypes.c_double * max(ns, 1))()
+    opts = Opts(device, win, int(graph), _fptr(recs), offs, ms)
+    _check(lib().a3d_run_batch(ctypes.byref(pb), arr, ns, ctypes.byref(opts)))
+    out = [recs[offs[i]:offs[i] + dims[i][0] * dims[i][1] * cfg.nt].reshape(dims[i][0], dims[i][1], cfg.nt)
+           for i in range(ns)]
+    return out, [ms[i] for i in range(ns)]

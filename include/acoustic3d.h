@@ -143,6 +143,40 @@ int a3d_forward_host(const a3d_config *cfg, const float *vel, const float *rho, 
                      const float *del, const float *theta, const float *phi,
                      const a3d_shot *shots, int nshot, float *recs_host, int device);
 
+/* ------------------------------------------------- batched multi-shot API */
+/* The batched entry point the reference's Python driver would feed instead of one
+ * process per shot (readmodel.py:186-204 runs a process pool over the shot list,
+ * each process calling one of the four entry points above once).  One call runs
+ * every shot of a survey on one device: the model is uploaded once per window
+ * shape, the autotuned launch shapes are kept for the whole batch, and each shot's
+ * record lands in recs_host. */
+typedef struct {
+    a3d_config cfg;    /* physics, whole-model grid, time axis, absorber, storage, tile */
+    const float *vel, *rho, *eps, *del, *theta, *phi;  /* host model arrays, nx*ny*nz
+                                                          each (NULL where not read) */
+} a3d_problem;
+
+typedef struct {
+    int x0, y0, z0;    /* window origin in model cells                              */
+    int nx, ny, nz;    /* window size; nx == 0 selects the whole model              */
+} a3d_window;
+
+typedef struct {
+    int device;                 /* CUDA device                                         */
+    const a3d_window *windows;  /* one per shot, or NULL (every shot sees the whole
+                                   model).  A windowed shot runs on the model cropped to
+                                   its window, with the window's own absorber; its
+                                   position stays in model cells and must lie inside   */
+    int graph;                  /* 1: replay each shot's time loop as one CUDA graph   */
+    float *recs_host;           /* out (or NULL): the records one after another, shot i
+                                   taking nt * wnx * wny floats ([wny][wnx][nt])        */
+    size_t *rec_offsets;        /* out (or NULL): nshot float offsets into recs_host   */
+    double *ms;                 /* out (or NULL): nshot device times of the time loops */
+} a3d_opts;
+
+/* Run nshot shots.  Returns A3D_OK, or the first failure (later shots not run). */
+int a3d_run_batch(const a3d_problem *pb, const a3d_shot *shots, int nshot, const a3d_opts *opts);
+
 /* Per-kernel device timing (CUDA events around every launch, on the engine's
  * stream).  After runs with profiling on, ms[0]/launches[0] sum the velocity
  * sweeps (1st order) or the fused steps (2nd order), ms[1]/launches[1] the stress

@@ -48,3 +48,17 @@ def test_unsupported_storage_rejected(engine_lib):
     h = ctypes.c_void_p()
     rc = a3d.lib().a3d_engine_create(ctypes.byref(h), ctypes.byref(cfg), *[a3d._fptr(None)] * 6, 0)
     assert rc == a3d.A3D_E_UNSUPPORTED
+
+
+def test_batch_rejects_bad_windows_without_gpu(engine_lib):
+    """a3d_run_batch checks every window and shot before it touches a device."""
+    import a3d
+    import numpy as np
+    cfg = a3d.make_config("iso", 12, 10, 8, nt=10)
+    m = {"vel": np.full((10, 12, 8), 2000, np.float32), "rho": np.full((10, 12, 8), 2000, np.float32)}
+    with pytest.raises(a3d.A3DError) as ei:
+        a3d.run_batch(cfg, m, [(2, 2, 2)], windows=[(6, 0, 0, 8, 10, 8)])  # x0 + nx > 12
+    assert ei.value.code == a3d.A3D_E_ARG and "outside the 12x10x8 model" in str(ei.value)
+    with pytest.raises(a3d.A3DError) as ei:
+        a3d.run_batch(cfg, m, [(1, 2, 2)], windows=[(2, 0, 0, 8, 10, 8)])  # shot left of its window
+    assert ei.value.code == a3d.A3D_E_ARG and "outside its window" in str(ei.value)
