@@ -390,17 +390,18 @@ int a3d_engine::autotune() {
     std::vector<std::pair<int, int>> shapes;
     if (multirow) shapes = {{8, 1}, {16, 1}, {8, 2}, {16, 2}, {16, 4}};
     else shapes = {{8, 1}, {16, 1}};
-    // A3D_TUNE="tx,rows,deep,plan[;tx,rows,deep,plan]" pins the launch configuration of
+    // A3D_TUNE="tx,rows,depth,plan[;tx,rows,depth,plan]" pins the launch configuration of
     // each kernel kind (velocity; stress) instead of timing candidates
     if (const char *env = getenv("A3D_TUNE"); env && *env && !fp64) {
         const char *q = env;
         for (int k = 0; k < 2; ++k) {
-            int tx = 0, rows = 0, deep = 0, mode = 0, n = 0;
-            if (sscanf(q, "%d,%d,%d,%d%n", &tx, &rows, &deep, &mode, &n) != 4 || (tx != 8 && tx != 16) ||
+            int tx = 0, rows = 0, depth = 0, mode = 0, n = 0;
+            if (sscanf(q, "%d,%d,%d,%d%n", &tx, &rows, &depth, &mode, &n) != 4 || (tx != 8 && tx != 16) ||
+                depth < 0 || depth > (multirow ? 2 : 1) ||
                 (rows != 1 && rows != 2 && rows != 4) || (rows == 4 && tx != 16) || mode < 0 || mode > 1)
-                return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,deep,plan[;...], got \"%s\"", env);
+                return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[;...], got \"%s\"", env);
             if (!multirow && rows != 1) return fail(A3D_E_ARG, "A3D_TUNE: this physics runs one row per warp");
-            tune[k] = Tune{tx, deep != 0, mode, rows};
+            tune[k] = Tune{tx, depth, mode, rows};
             tune[k].ms = 0;
             q += n;
             if (*q == ';') ++q;
@@ -410,12 +411,12 @@ int a3d_engine::autotune() {
         return A3D_OK;
     }
     if (c.tile_x < 0 || fp64) {  // fixed defaults (and the FP64 run): 32x8, shallow rings, both plans
-        for (int m = 0; m < 2; ++m) cand.push_back(Tune{8, false, m, multirow ? 2 : 1});
+        for (int m = 0; m < 2; ++m) cand.push_back(Tune{8, 0, m, multirow ? 2 : 1});
     } else {
         for (auto sh : shapes)
-            for (int d = 0; d < 2; ++d)
+            for (int d = 0; d <= (multirow ? 2 : 1); ++d)
                 for (int m = 0; m < 2; ++m)
-                    if (!fixed_tx || sh.first == fixed_tx) cand.push_back(Tune{sh.first, d != 0, m, sh.second});
+                    if (!fixed_tx || sh.first == fixed_tx) cand.push_back(Tune{sh.first, d, m, sh.second});
     }
     const int kinds = c.physics == A3D_2ORDER ? 1 : 2;
     cudaEvent_t t0, t1;
@@ -428,7 +429,7 @@ int a3d_engine::autotune() {
             auto launch_once = [&]() -> cudaError_t {
                 if (c.physics == A3D_2ORDER) {
                     K2OLaunch L{};
-                    L.tx = tc.tx; L.deep = tc.deep; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
+                    L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
                     L.tm_cur = m2o_cur[ti][0]; L.tm_prev = m2o_prev[ti][1]; L.tm_vv = m2o_vv[ti];
                     L.ybuf = Y;
                     K2OParams &p = L.p;
@@ -459,7 +460,7 @@ int a3d_engine::autotune() {
                 L.maps = k == 0 ? mvel[ti] : mstr[ti];
                 L.nmaps = k == 0 ? nvel : nstr;
                 L.out0 = k == 0 ? u : P; L.out1 = k == 0 ? v : Q; L.out2 = w;
-                L.tx = tc.tx; L.deep = tc.deep; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
+                L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
                 auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
                 return launch(L, st);
             };
@@ -567,7 +568,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         K2OLaunch L{};
         const int ti = tune[0].tx == 16 ? 1 : 0;
         L.tx = tune[0].tx;
-        L.deep = tune[0].deep;
+        L.depth = tune[0].depth;
         L.mode = tune[0].mode;
         L.rows = tune[0].rows;
         L.fp64 = fp64;
@@ -634,8 +635,8 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         Ls.maps = mstr[tune[1].tx == 16 ? 1 : 0]; Ls.nmaps = nstr;
         Lv.out0 = u; Lv.out1 = v; Lv.out2 = w;
         Ls.out0 = P; Ls.out1 = Q;
-        Lv.tx = tune[0].tx; Lv.deep = tune[0].deep; Lv.mode = tune[0].mode; Lv.rows = tune[0].rows;
-        Ls.tx = tune[1].tx; Ls.deep = tune[1].deep; Ls.mode = tune[1].mode; Ls.rows = tune[1].rows;
+        Lv.tx = tune[0].tx; Lv.depth = tune[0].depth; Lv.mode = tune[0].mode; Lv.rows = tune[0].rows;
+        Ls.tx = tune[1].tx; Ls.depth = tune[1].depth; Ls.mode = tune[1].mode; Ls.rows = tune[1].rows;
         Lv.fp64 = Ls.fp64 = fp64; Lv.grid = Ls.grid = 0;
         auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
         if ((rc = prepare_profiling(this, 3))) return rc;
@@ -826,11 +827,11 @@ extern "C" int a3d_engine_describe(a3d_engine *e, char *buf, size_t n) {
     }
     snprintf(buf, n,
              "{\"grid\": [%d, %d, %d], \"ldz\": %d, \"pad\": %d, \"device_bytes\": %zu, "
-             "\"kernels\": [{\"tile_x\": %d, \"rows\": %d, \"deep\": %d, \"plan\": %d, \"ms\": %.4f}, "
-             "{\"tile_x\": %d, \"rows\": %d, \"deep\": %d, \"plan\": %d, \"ms\": %.4f}]}",
+             "\"kernels\": [{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"ms\": %.4f}, "
+             "{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"ms\": %.4f}]}",
              e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, e->tune[0].tx, e->tune[0].rows,
-             (int)e->tune[0].deep, e->tune[0].mode, e->tune[0].ms, e->tune[1].tx, e->tune[1].rows,
-             (int)e->tune[1].deep, e->tune[1].mode, e->tune[1].ms);
+             e->tune[0].depth, e->tune[0].mode, e->tune[0].ms, e->tune[1].tx, e->tune[1].rows,
+             e->tune[1].depth, e->tune[1].mode, e->tune[1].ms);
     return A3D_OK;
 }
 

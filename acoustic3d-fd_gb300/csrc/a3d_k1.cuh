@@ -41,7 +41,7 @@ struct K1Launch {
     K1Params p;
     int tx, grid;
     bool fp64;
-    bool deep;  // deep TMA rings
+    int depth;  // TMA ring depth (0, 1, 2: see Ring in a3d_pipe.cuh; VTI/TTI: 0, 1)
     int mode;   // sweep plan (plan_sweep)
     int rows;   // tile rows per consumer warp (iso: 2 or 4; VTI/TTI: 1)
 };

@@ -93,4 +93,26 @@ static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid,
 // loads of a stored field value / smem tile element as the arithmetic type
 template <class T, class S> __device__ __forceinline__ T ld(const S *a, int i) { return from_store<T, S>(a[i]); }
 
+// Two z-adjacent cells per lane: elements i, i+1 (i even, so the pair is aligned)
+// move as one 8-byte (float) or 16-byte (double) access.
+template <class T> struct Two { T a, b; };
+template <class S> struct Vec2;
+template <> struct Vec2<float> { using t = float2; };
+template <> struct Vec2<double> { using t = double2; };
+template <class T, class S> __device__ __forceinline__ Two<T> ld2(const S *p, int i) {
+    const auto v = *reinterpret_cast<const typename Vec2<S>::t *>(p + i);
+    return Two<T>{(T)v.x, (T)v.y};
+}
+template <class S, class T> __device__ __forceinline__ void st2(S *p, uint32_t i, T a, T b) {
+    typename Vec2<S>::t v;
+    v.x = to_store<S, T>(a);
+    v.y = to_store<S, T>(b);
+    *reinterpret_cast<typename Vec2<S>::t *>(p + i) = v;
+}
+// store the pair, or only its first element when the second lies past the sweep
+template <class S, class T> __device__ __forceinline__ void st2m(S *p, uint32_t i, T a, T b, bool both) {
+    if (both) st2<S, T>(p, i, a, b);
+    else p[i] = to_store<S, T>(a);
+}
+
 }  // namespace a3d

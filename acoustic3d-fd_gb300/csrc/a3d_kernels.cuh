@@ -56,7 +56,7 @@ struct K2OLaunch {
     int tx;      // tile width along x (8, 16)
     int grid;    // CTAs (0: planned from the occupancy)
     bool fp64;
-    bool deep;   // deep TMA rings (16 + 8 stages) instead of 8 + 4
+    int depth;   // TMA ring depth (0, 1, 2: see Ring in a3d_pipe.cuh)
     int mode;    // sweep plan (plan_sweep)
     int rows;    // tile rows per consumer warp (2 or 4)
 };

@@ -21,27 +21,30 @@ namespace a3d {
 // iso_vel: maps {P (box H), u, v, w (core), 1/rho (core, float)}
 template <int TX, class S, int D>
 struct IsoVelL {
-    static constexpr int KA = Depth<D>::KA, KB = Depth<D>::KB;
     static constexpr int AW = 40, AH = TX + 8;
     static constexpr uint32_t A_BYTES = AW * AH * sizeof(S);
     static constexpr uint32_t C = 32 * TX;  // core elements
     static constexpr uint32_t B_BYTES = 3 * C * sizeof(S) + C * 4;
     static constexpr size_t A_STRIDE = (A_BYTES + 127) / 128 * 128;
     static constexpr size_t B_STRIDE = (B_BYTES + 127) / 128 * 128;
-    static constexpr size_t BAR_OFF = KA * A_STRIDE + KB * B_STRIDE;
-    static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBarsM<KA, KB>);
+    using RG = Ring<D, A_STRIDE, B_STRIDE>;
+    using Bars = typename RG::Bars;
+    static constexpr int KA = RG::KA, KB = RG::KB;
+    static constexpr size_t RB = RG::RB, B_OFF = RG::B_OFF, BAR_OFF = RG::BAR_OFF, TOTAL = RG::TOTAL;
 };
 
 template <int TX, class S, int D, int R>
-__global__ void __launch_bounds__(32 * (TX / R) + 32)
+__global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     iso_vel(const __grid_constant__ Maps<5> mp, S *__restrict__ u, S *__restrict__ v,
             S *__restrict__ w, const __grid_constant__ K1Params p) {
     using L = IsoVelL<TX, S, D>;
     using T = typename Arith<S>::T;
-    constexpr int NW = TX / R, NC = 32 * NW, AW = L::AW;
+    using T2 = Two<T>;
+    constexpr int NW = TX / (2 * R), NC = 32 * NW, AW = L::AW;
+    static_assert(NW >= 1, "a warp covers 2R tile rows");
     extern __shared__ __align__(128) unsigned char smem[];
-    auto &bars = *reinterpret_cast<PipeBarsM<L::KA, L::KB> *>(smem + L::BAR_OFF);
-    unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
+    auto &bars = *reinterpret_cast<typename L::Bars *>(smem + L::BAR_OFF);
+    unsigned char *ringA = smem, *ringB = smem + L::B_OFF;
     if (threadIdx.x == 0) bars.init(NW);
     __syncthreads();
     long long w0, w1;
@@ -49,15 +52,15 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
     if (w0 >= w1) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    if (warp == NW) {
+    if (warp == NW) {  // producer warp: one thread issues every copy
         if (lane != 0) return;
         for (int i = 0; i < 5; ++i) prefetch_tmap(&mp.m[i]);
-        pipe_produce_m<TX, L::KA, L::KB>(
-            p.sw, w0, w1, bars, p.err, [&](uint32_t sa, int sb, uint64_t *bar, const Seg &s, int q) {
-                mbar_arrive_expect_tx(bar, L::A_BYTES + (sb >= 0 ? L::B_BYTES : 0u));
+        pipe_produce_m<TX, L::KA, L::KB, L::RB>(
+            p.sw, w0, w1, bars, ringB, p.err, [](const Seg &, int) { return (uint32_t)L::B_STRIDE; },
+            [&](uint32_t sa, unsigned char *dst, uint32_t, uint64_t *bar, const Seg &s, int q) {
+                mbar_arrive_expect_tx(bar, L::A_BYTES + (dst ? L::B_BYTES : 0u));
                 tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0 - MM, s.x0 - MM, q);
-                if (sb < 0) return;
-                unsigned char *dst = ringB + sb * L::B_STRIDE;
+                if (!dst) return;
                 const int o = q - MM;
                 tma_load_3d(dst, &mp.m[1], bar, s.z0, s.x0, o);
                 tma_load_3d(dst + L::C * sizeof(S), &mp.m[2], bar, s.z0, s.x0, o);
@@ -67,13 +70,19 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
         return;
     }
 
-    const int tz = lane, xw = warp * R;  // this warp's first tile row
-    const int c0 = (xw + MM) * AW + tz + MM;  // this thread's first cell in an A tile
-    T win[R][8];                              // P at the last 8 planes, slot = item mod 8
-    bool act[R];
-    T cx1d[R], cx2[R], cz1d = 0, cz2 = 0;
-    uint32_t gb[R];  // in-plane offsets of this thread's cells
+    // lane: z cells zl, zl+1 of the tile (zl = 2 (lane mod 16)) in tile rows
+    // xw .. xw+R-1, where the two half-warps take consecutive groups of R rows
+    const int zl = 2 * (lane & 15), xw = warp * 2 * R + (lane >> 4) * R;
+    const int c0 = (xw + MM) * AW + zl + MM;  // this lane's first cell pair in an A tile
+    T2 win[R][8];                             // P at the last 8 planes, slot = item mod 8
+    bool act[R], both = true;
+    T cx1d[R], cx2[R];
+    T2 cz1d{0, 0}, cz2{0, 0};
+    uint32_t gb[R];  // in-plane offsets of this lane's first cell per row
     int srcq = INT_MIN;
+    // y coefficients of the next output plane, loaded one plane ahead so that their
+    // global-load latency overlaps the current plane's work
+    float cy1n = 0, cy2n = 0;
     const uint32_t pstride = (uint32_t)p.ldz * (uint32_t)p.nnx;
     const T k[4] = {(T)C8_0, (T)C8_1, (T)C8_2, (T)C8_3};
     // the dipole enters the sweep's view of P (..iso..:94): patch the A tile of the
@@ -90,13 +99,14 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
         consumer_sync(NC);
     };
     pipe_run<TX, L::KA, L::KB, MM>(
-        p.sw, w0, w1, bars, p.err,
+        p.sw, w0, w1, bars, ringB, p.err,
         [&](const Seg &s) {
-            const int iz = s.z0 + tz;
+            const int iz = s.z0 + zl;
             const bool zact = iz < p.nnz - MM;
-            const int cz = min(iz, p.nnz - 1);
-            cz1d = (T)p.cz1[cz] * (T)p.dtz;
-            cz2 = (T)p.cz2[cz];
+            both = iz + 1 < p.nnz - MM;
+            const int cza = min(iz, p.nnz - 1), czb = min(iz + 1, p.nnz - 1);
+            cz1d = T2{(T)p.cz1[cza] * (T)p.dtz, (T)p.cz1[czb] * (T)p.dtz};
+            cz2 = T2{(T)p.cz2[cza], (T)p.cz2[czb]};
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int ix = s.x0 + xw + r;
@@ -108,97 +118,121 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
             }
             const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - MM);
             srcq = (p.inj && lx >= 0 && lx < L::AH && lz + 2 >= 0 && lz < AW) ? p.s_y : INT_MIN;
+            cy1n = p.cy1[s.ya];
+            cy2n = p.cy2[s.ya];
         },
         [&](auto ph, uint32_t sa, const Seg &s, int q) {
             constexpr int P = decltype(ph)::value;
             S *A = reinterpret_cast<S *>(ringA + sa * L::A_STRIDE);
             if (q == srcq) inject(A, s);
 #pragma unroll
-            for (int r = 0; r < R; ++r) win[r][P] = ld<T>(A, c0 + r * AW);
+            for (int r = 0; r < R; ++r) win[r][P] = ld2<T>(A, c0 + r * AW);
         },
-        [&](int ph, uint32_t sa, uint32_t sh, uint32_t sb, const Seg &s, int q) {
+        [&](int ph, uint32_t sa, uint32_t sh, const unsigned char *sbp, const Seg &s, int q) {
             S *A = reinterpret_cast<S *>(ringA + sa * L::A_STRIDE);
             if (q == srcq) inject(A, s);
             // window push of P(q) and the y-derivative at o = q - 4 (..iso..:126)
-            T yy[R];
+            T2 yy[R];
             with_phase(ph, [&](auto pc) {
                 constexpr int P = decltype(pc)::value;
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    win[r][P] = ld<T>(A, c0 + r * AW);
-                    T a = 0;
+                    win[r][P] = ld2<T>(A, c0 + r * AW);
+                    T a = 0, b = 0;
 #pragma unroll
-                    for (int im = 0; im < 4; ++im)  // P(o+1+m) in slot (P+5+m)&7, P(o-m) in (P+4-m)&7
-                        a = fma_t(k[im], win[r][(P + 5 + im) & 7] - win[r][(P + 4 - im) & 7], a);
-                    yy[r] = a;
+                    for (int im = 0; im < 4; ++im) {  // P(o+1+m) in slot (P+5+m)&7, P(o-m) in (P+4-m)&7
+                        const T2 hi = win[r][(P + 5 + im) & 7], lo = win[r][(P + 4 - im) & 7];
+                        a = fma_t(k[im], hi.a - lo.a, a);
+                        b = fma_t(k[im], hi.b - lo.b, b);
+                    }
+                    yy[r] = T2{a, b};
                 }
             });
             // output plane o = q - 4: its P tile is the A stage held since item q - 4
             const int o = q - MM;
             const S *Ao = reinterpret_cast<const S *>(ringA + sh * L::A_STRIDE);
-            const unsigned char *sbp = ringB + sb * L::B_STRIDE;
             const S *Bu = reinterpret_cast<const S *>(sbp);
             const S *Bv = Bu + L::C, *Bw = Bu + 2 * L::C;
             const float *Br = reinterpret_cast<const float *>(sbp + 3 * L::C * sizeof(S));
-            // P at tile rows xw+1 .. xw+R+7 of this z column: xs[j] = P(x = xw - 3 + j)
-            T xs[R + 7];
+            // P at tile rows xw+1 .. xw+R+7 of this lane's z pair: xs[j] = P(x = xw - 3 + j)
+            T2 xs[R + 7];
 #pragma unroll
-            for (int j = 0; j < R + 7; ++j) xs[j] = ld<T>(Ao, c0 + (j + 1 - MM) * AW);
-            const T cy1d = (T)p.cy1[o] * (T)p.dty, cy2 = (T)p.cy2[o];
+            for (int j = 0; j < R + 7; ++j) xs[j] = ld2<T>(Ao, c0 + (j + 1 - MM) * AW);
+            const T cy1d = (T)cy1n * (T)p.dty, cy2 = (T)cy2n;
+            cy1n = p.cy1[o + 1];  // o + 1 <= nny - 4: in bounds
+            cy2n = p.cy2[o + 1];
             const uint32_t po = pstride * (uint32_t)o;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const int c = c0 + r * AW, bi = (xw + r) * 32 + tz;
-                T xx = 0, zz = 0;
+                const int bi = (xw + r) * 32 + zl;
+                // P along z at halo'd row positions zl .. zl+9 (position zl+4 = cell a)
+                T2 zp[5];
+#pragma unroll
+                for (int m = 0; m < 5; ++m) zp[m] = ld2<T>(Ao, c0 + r * AW - MM + 2 * m);
+                const T zv[10] = {zp[0].a, zp[0].b, zp[1].a, zp[1].b, zp[2].a,
+                                  zp[2].b, zp[3].a, zp[3].b, zp[4].a, zp[4].b};
+                T xa = 0, xb = 0, za = 0, zb = 0;
 #pragma unroll
                 for (int im = 0; im < 4; ++im) {  // ..iso..:125-127
-                    xx = fma_t(k[im], xs[r + 4 + im] - xs[r + 3 - im], xx);
-                    zz = fma_t(k[im], ld<T>(Ao, c + im + 1) - ld<T>(Ao, c - im), zz);
+                    xa = fma_t(k[im], xs[r + 4 + im].a - xs[r + 3 - im].a, xa);
+                    xb = fma_t(k[im], xs[r + 4 + im].b - xs[r + 3 - im].b, xb);
+                    za = fma_t(k[im], zv[5 + im] - zv[4 - im], za);
+                    zb = fma_t(k[im], zv[6 + im] - zv[5 - im], zb);
                 }
-                const T ri = (T)Br[bi];  // 1/rho
-                xx = xx * ri;
-                const T yr = yy[r] * ri;
-                zz = zz * ri;
-                const T un = fma_t(cx2[r], ld<T>(Bu, bi), -(cx1d[r] * xx));
-                const T vn = fma_t(cy2, ld<T>(Bv, bi), -(cy1d * yr));
-                const T wn = fma_t(cz2, ld<T>(Bw, bi), -(cz1d * zz));
+                const float2 ri = *reinterpret_cast<const float2 *>(Br + bi);  // 1/rho
+                const T2 uo = ld2<T>(Bu, bi), vo = ld2<T>(Bv, bi), wo = ld2<T>(Bw, bi);
+                xa = xa * (T)ri.x;
+                xb = xb * (T)ri.y;
+                const T ya = yy[r].a * (T)ri.x, yb = yy[r].b * (T)ri.y;
+                za = za * (T)ri.x;
+                zb = zb * (T)ri.y;
+                const T una = fma_t(cx2[r], uo.a, -(cx1d[r] * xa)), unb = fma_t(cx2[r], uo.b, -(cx1d[r] * xb));
+                const T vna = fma_t(cy2, vo.a, -(cy1d * ya)), vnb = fma_t(cy2, vo.b, -(cy1d * yb));
+                const T wna = fma_t(cz2.a, wo.a, -(cz1d.a * za)), wnb = fma_t(cz2.b, wo.b, -(cz1d.b * zb));
                 if (act[r]) {
                     const uint32_t g = gb[r] + po;
-                    u[g] = to_store<S, T>(un);
-                    v[g] = to_store<S, T>(vn);
-                    w[g] = to_store<S, T>(wn);
+                    st2m<S, T>(u, g, una, unb, both);
+                    st2m<S, T>(v, g, vna, vnb, both);
+                    st2m<S, T>(w, g, wna, wnb, both);
                 }
             }
         });
 }
+
 
 // ===========================================================================
 // iso_stress: maps {v (core), u (box HX), w (box HZ), P (core), rho, vp (core, float),
 //                   px, py, pz (core; loaded only for tiles/planes on a damped axis)}
 template <int TX, class S, int D>
 struct IsoStrL {
-    static constexpr int KA = Depth<D>::KA, KB = Depth<D>::KB;
     static constexpr uint32_t C = 32 * TX;
     static constexpr uint32_t UX = 32 * (TX + 8), WZ = 40 * TX;
     static constexpr uint32_t A_BYTES = C * sizeof(S);
+    // fixed part of a B item (u, w, P, rho, vp), then one tile per damped axis
     static constexpr uint32_t B_FIXED = (UX + WZ + C) * sizeof(S) + 2 * C * 4;
-    static constexpr uint32_t B_BYTES = B_FIXED + 3 * C * sizeof(S);
+    static constexpr uint32_t AUX = C * sizeof(S);
+    static constexpr uint32_t B_BYTES = B_FIXED + 3 * AUX;
     static constexpr size_t A_STRIDE = (A_BYTES + 127) / 128 * 128;
     static constexpr size_t B_STRIDE = (B_BYTES + 127) / 128 * 128;
-    static constexpr size_t BAR_OFF = KA * A_STRIDE + KB * B_STRIDE;
-    static constexpr size_t TOTAL = BAR_OFF + sizeof(PipeBarsM<KA, KB>);
+    static_assert(B_FIXED % 128 == 0 && AUX % 128 == 0, "B item parts are 128-byte aligned");
+    using RG = Ring<D, A_STRIDE, B_STRIDE>;
+    using Bars = typename RG::Bars;
+    static constexpr int KA = RG::KA, KB = RG::KB;
+    static constexpr size_t RB = RG::RB, B_OFF = RG::B_OFF, BAR_OFF = RG::BAR_OFF, TOTAL = RG::TOTAL;
 };
 
 template <int TX, class S, int D, int R>
-__global__ void __launch_bounds__(32 * (TX / R) + 32)
+__global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     iso_stress(const __grid_constant__ Maps<9> mp, S *__restrict__ P,
                const __grid_constant__ K1Params p) {
     using L = IsoStrL<TX, S, D>;
     using T = typename Arith<S>::T;
-    constexpr int NW = TX / R;
+    using T2 = Two<T>;
+    constexpr int NW = TX / (2 * R);
+    static_assert(NW >= 1, "a warp covers 2R tile rows");
     extern __shared__ __align__(128) unsigned char smem[];
-    auto &bars = *reinterpret_cast<PipeBarsM<L::KA, L::KB> *>(smem + L::BAR_OFF);
-    unsigned char *ringA = smem, *ringB = smem + L::KA * L::A_STRIDE;
+    auto &bars = *reinterpret_cast<typename L::Bars *>(smem + L::BAR_OFF);
+    unsigned char *ringA = smem, *ringB = smem + L::B_OFF;
     if (threadIdx.x == 0) bars.init(NW);
     __syncthreads();
     long long w0, w1;
@@ -208,60 +242,66 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
     constexpr size_t oW = L::UX * sizeof(S), oP = (L::UX + L::WZ) * sizeof(S),
                      oR = (L::UX + L::WZ + L::C) * sizeof(S), oV = oR + L::C * 4,
                      oX = L::B_FIXED;  // px, py, pz tiles follow the fixed part
-    constexpr uint32_t AUX = L::C * sizeof(S);
+    constexpr uint32_t AUX = L::AUX;
 
-    if (warp == NW) {
+    if (warp == NW) {  // producer warp: one thread issues every copy
         if (lane != 0) return;
         for (int i = 0; i < 9; ++i) prefetch_tmap(&mp.m[i]);
-        pipe_produce_m<TX, L::KA, L::KB>(
-            p.sw, w0, w1, bars, p.err, [&](uint32_t sa, int sb, uint64_t *bar, const Seg &s, int q) {
-                if (sb < 0) {
-                    mbar_arrive_expect_tx(bar, L::A_BYTES);
-                    tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0, s.x0, q);
-                    return;
-                }
-                const int o = q - MM;
-                const bool nx_ = range_damped(s.x0, TX, p.ulo[0], p.uhi[0]);
-                const bool ny_ = range_damped(o, 1, p.ulo[1], p.uhi[1]);
-                const bool nz_ = range_damped(s.z0, 32, p.ulo[2], p.uhi[2]);
-                mbar_arrive_expect_tx(bar, L::A_BYTES + L::B_FIXED + AUX * ((int)nx_ + (int)ny_ + (int)nz_));
+        // split components only for tiles / planes on a damped axis, packed after the
+        // fixed part in x, y, z order
+        auto naux = [&](const Seg &s, int o) {
+            return (uint32_t)range_damped(s.x0, TX, p.ulo[0], p.uhi[0]) +
+                   (uint32_t)range_damped(o, 1, p.ulo[1], p.uhi[1]) +
+                   (uint32_t)range_damped(s.z0, 32, p.ulo[2], p.uhi[2]);
+        };
+        pipe_produce_m<TX, L::KA, L::KB, L::RB>(
+            p.sw, w0, w1, bars, ringB, p.err, [&](const Seg &s, int o) { return L::B_FIXED + AUX * naux(s, o); },
+            [&](uint32_t sa, unsigned char *dst, uint32_t bbytes, uint64_t *bar, const Seg &s, int q) {
+                mbar_arrive_expect_tx(bar, L::A_BYTES + bbytes);
                 tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0, s.x0, q);
-                unsigned char *dst = ringB + sb * L::B_STRIDE;
+                if (!dst) return;
+                const int o = q - MM;
                 tma_load_3d(dst, &mp.m[1], bar, s.z0, s.x0 - MM, o);
                 tma_load_3d(dst + oW, &mp.m[2], bar, s.z0 - MM, s.x0, o);
                 tma_load_3d(dst + oP, &mp.m[3], bar, s.z0, s.x0, o);
                 tma_load_3d(dst + oR, &mp.m[4], bar, s.z0, s.x0, o);
                 tma_load_3d(dst + oV, &mp.m[5], bar, s.z0, s.x0, o);
-                if (nx_) tma_load_3d(dst + oX, &mp.m[6], bar, s.z0, s.x0, o);
-                if (ny_) tma_load_3d(dst + oX + AUX, &mp.m[7], bar, s.z0, s.x0, o);
-                if (nz_) tma_load_3d(dst + oX + 2 * AUX, &mp.m[8], bar, s.z0, s.x0, o);
+                unsigned char *ax = dst + oX;
+                if (range_damped(s.x0, TX, p.ulo[0], p.uhi[0])) { tma_load_3d(ax, &mp.m[6], bar, s.z0, s.x0, o); ax += AUX; }
+                if (range_damped(o, 1, p.ulo[1], p.uhi[1])) { tma_load_3d(ax, &mp.m[7], bar, s.z0, s.x0, o); ax += AUX; }
+                if (range_damped(s.z0, 32, p.ulo[2], p.uhi[2])) tma_load_3d(ax, &mp.m[8], bar, s.z0, s.x0, o);
             });
         return;
     }
 
-    const int tz = lane, xw = warp * R;
-    T win[R][8];  // v at the last 8 planes, slot = item mod 8
-    bool dzm = false, act[R], dxm[R], rec[R];
-    float ax1[R], ax2[R], az1 = 1, az2 = 1;
+    // lane: z cells zl, zl+1 of the tile (zl = 2 (lane mod 16)) in tile rows
+    // xw .. xw+R-1, where the two half-warps take consecutive groups of R rows
+    const int zl = 2 * (lane & 15), xw = warp * 2 * R + (lane >> 4) * R;
+    T2 win[R][8];  // v at the last 8 planes, slot = item mod 8
+    bool act[R], dxm[R], reca[R], recb[R], both = true, dza = false, dzb = false;
+    float ax1[R], ax2[R];
+    float2 az1{1, 1}, az2{1, 1};
     uint32_t gb[R];
-    int trb[R];  // receiver trace index of this cell at y = npml, or -1
-    bool fast = false;  // tile undamped in x and z, every cell active, no receivers
-    uint32_t g0 = 0;    // in-plane offset of this thread's first cell
+    int trb[R];          // receiver trace index of this lane's row, ix - npml
+    bool fast = false;   // tile undamped in x and z, every cell active, no receivers
+    bool tdx = false, tdz = false;  // the tile touches the damped x / z range (split tiles loaded)
+    float ay1n = 1, ay2n = 1;        // y coefficients of the next output plane (loaded one ahead)
     S *px = reinterpret_cast<S *>(p.px), *py = reinterpret_cast<S *>(p.py),
       *pz = reinterpret_cast<S *>(p.pz);
     const uint32_t pstride = (uint32_t)p.ldz * (uint32_t)p.nnx;
     const T k[4] = {(T)C8_0, (T)C8_1, (T)C8_2, (T)C8_3};
     const T dtx = (T)p.dtx, dty = (T)p.dty, dtz = (T)p.dtz;
     pipe_run<TX, L::KA, L::KB, 0>(
-        p.sw, w0, w1, bars, p.err,
+        p.sw, w0, w1, bars, ringB, p.err,
         [&](const Seg &s) {
-            const int iz = s.z0 + tz;
+            const int iz = s.z0 + zl;
             const bool zact = iz < p.nnz - MM;
-            const int cz = min(iz, p.nnz - 1);
-            az1 = p.az1[cz];
-            az2 = p.az2[cz];
-            dzm = damped(az1, az2);
-            const bool rec_z = iz == p.npml;
+            both = iz + 1 < p.nnz - MM;
+            const int cza = min(iz, p.nnz - 1), czb = min(iz + 1, p.nnz - 1);
+            az1 = float2{p.az1[cza], p.az1[czb]};
+            az2 = float2{p.az2[cza], p.az2[czb]};
+            dza = damped(az1.x, az2.x);
+            dzb = damped(az1.y, az2.y);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int ix = s.x0 + xw + r;
@@ -270,113 +310,140 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
                 ax1[r] = p.ax1[cxi];
                 ax2[r] = p.ax2[cxi];
                 dxm[r] = damped(ax1[r], ax2[r]);
-                rec[r] = act[r] && rec_z && ix >= p.npml && ix < p.npml + p.nx;
+                const bool rx = act[r] && ix >= p.npml && ix < p.npml + p.nx;
+                reca[r] = rx && iz == p.npml;
+                recb[r] = rx && both && iz + 1 == p.npml;
                 trb[r] = ix - p.npml;
                 gb[r] = (uint32_t)iz + (uint32_t)p.ldz * (uint32_t)cxi;
             }
-            g0 = gb[0];
-            fast = !range_damped(s.x0, TX, p.ulo[0], p.uhi[0]) && !range_damped(s.z0, 32, p.ulo[2], p.uhi[2]) &&
-                   !(p.npml >= s.z0 && p.npml < s.z0 + 32);
+            tdx = range_damped(s.x0, TX, p.ulo[0], p.uhi[0]);
+            tdz = range_damped(s.z0, 32, p.ulo[2], p.uhi[2]);
+            fast = !tdx && !tdz && !(p.npml >= s.z0 && p.npml < s.z0 + 32);
+            ay1n = p.ay1[s.ya];
+            ay2n = p.ay2[s.ya];
         },
         [&](auto ph, uint32_t sa, const Seg &, int) {
             constexpr int Q = decltype(ph)::value;
             const S *A = reinterpret_cast<const S *>(ringA + sa * L::A_STRIDE);
 #pragma unroll
-            for (int r = 0; r < R; ++r) win[r][Q] = ld<T>(A, (xw + r) * 32 + tz);
+            for (int r = 0; r < R; ++r) win[r][Q] = ld2<T>(A, (xw + r) * 32 + zl);
         },
-        [&](int ph, uint32_t sa, uint32_t, uint32_t sb, const Seg &, int q) {
+        [&](int ph, uint32_t sa, uint32_t, const unsigned char *sbp, const Seg &, int q) {
             const int o = q - MM;
             // y-derivative at o from the window v(o-4 .. o+3) (plane o+m in slot
             // (ph+4+m)&7; ..iso..:179), then v(q) replaces v(q-8), which it last served
             const S *A = reinterpret_cast<const S *>(ringA + sa * L::A_STRIDE);
-            T yy[R];
+            T2 yy[R];
             with_phase(ph, [&](auto pc) {
                 constexpr int Q = decltype(pc)::value;
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    T a = 0;
+                    T ya = 0, yb = 0;
 #pragma unroll
-                    for (int im = 0; im < 4; ++im)
-                        a = fma_t(k[im], win[r][(Q + 4 + im) & 7] - win[r][(Q + 3 - im) & 7], a);
-                    yy[r] = a;
-                    win[r][Q] = ld<T>(A, (xw + r) * 32 + tz);
+                    for (int im = 0; im < 4; ++im) {
+                        const T2 hi = win[r][(Q + 4 + im) & 7], lo = win[r][(Q + 3 - im) & 7];
+                        ya = fma_t(k[im], hi.a - lo.a, ya);
+                        yb = fma_t(k[im], hi.b - lo.b, yb);
+                    }
+                    yy[r] = T2{ya, yb};
+                    win[r][Q] = ld2<T>(A, (xw + r) * 32 + zl);
                 }
             });
-            const unsigned char *sbp = ringB + sb * L::B_STRIDE;
             const S *Bu = reinterpret_cast<const S *>(sbp);
             const S *Bw = reinterpret_cast<const S *>(sbp + oW);
             const S *Bp = reinterpret_cast<const S *>(sbp + oP);
             const float *Br = reinterpret_cast<const float *>(sbp + oR);
             const float *Bvp = reinterpret_cast<const float *>(sbp + oV);
+            // split tiles as packed by the producer: x, then y, then z, present ones only
             const S *Bx = reinterpret_cast<const S *>(sbp + oX);
-            const S *By = Bx + L::C, *Bz = Bx + 2 * L::C;
-            // u at tile rows xw .. xw+R+6 of this z column: us[j] = u(x = xw - 4 + j)
-            T us[R + 7];
+            const S *By = Bx + (tdx ? L::C : 0u);
+            const S *Bz = By + ((o < p.ulo[1] || o >= p.uhi[1]) ? L::C : 0u);
+            // u at tile rows xw .. xw+R+6 of this lane's z pair: us[j] = u(x = xw - 4 + j)
+            T2 us[R + 7];
 #pragma unroll
-            for (int j = 0; j < R + 7; ++j) us[j] = ld<T>(Bu, (xw + j) * 32 + tz);
+            for (int j = 0; j < R + 7; ++j) us[j] = ld2<T>(Bu, (xw + j) * 32 + zl);
             const bool dym = o < p.ulo[1] || o >= p.uhi[1];  // == damped(ay1[o], ay2[o])
             const uint32_t po = pstride * (uint32_t)o;
+            const float ay1 = ay1n, ay2 = ay2n;
+            ay1n = p.ay1[o + 1];  // o + 1 <= nny - 4: in bounds
+            ay2n = p.ay2[o + 1];
+            // derivatives of row r: x from the u rows, z from the halo'd w row
+            // (positions zl .. zl+9, position zl+4 = cell a), ..iso..:178-180
+            auto deriv = [&](int r, T2 &xx, T2 &zz) {
+                T2 zp[5];
+#pragma unroll
+                for (int m = 0; m < 5; ++m) zp[m] = ld2<T>(Bw, (xw + r) * 40 + zl + 2 * m);
+                const T zv[10] = {zp[0].a, zp[0].b, zp[1].a, zp[1].b, zp[2].a,
+                                  zp[2].b, zp[3].a, zp[3].b, zp[4].a, zp[4].b};
+                T xa = 0, xb = 0, za = 0, zb = 0;
+#pragma unroll
+                for (int im = 0; im < 4; ++im) {
+                    xa = fma_t(k[im], us[r + 4 + im].a - us[r + 3 - im].a, xa);
+                    xb = fma_t(k[im], us[r + 4 + im].b - us[r + 3 - im].b, xb);
+                    za = fma_t(k[im], zv[4 + im] - zv[3 - im], za);
+                    zb = fma_t(k[im], zv[5 + im] - zv[4 - im], zb);
+                }
+                xx = T2{xa, xb};
+                zz = T2{za, zb};
+            };
             if (fast && !dym) {  // undamped interior tile and plane: P - gx - gy - gz, a1 == 1
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    const int bi = (xw + r) * 32 + tz, cw = (xw + r) * 40 + tz + MM;
-                    T xx = 0, zz = 0;
-#pragma unroll
-                    for (int im = 0; im < 4; ++im) {  // ..iso..:178-180
-                        xx = fma_t(k[im], us[r + 4 + im] - us[r + 3 - im], xx);
-                        zz = fma_t(k[im], ld<T>(Bw, cw + im) - ld<T>(Bw, cw - im - 1), zz);
-                    }
+                    const int bi = (xw + r) * 32 + zl;
+                    T2 xx, zz;
+                    deriv(r, xx, zz);
+                    const float2 rv = *reinterpret_cast<const float2 *>(Br + bi);
+                    const float2 vv = *reinterpret_cast<const float2 *>(Bvp + bi);
+                    const T2 Po = ld2<T>(Bp, bi);
                     // (((1 * rho) * vp) * vp) == (rho * vp) * vp  (..iso..:182-184)
-                    const T t = ((T)Br[bi] * (T)Bvp[bi]) * (T)Bvp[bi];
-                    const T gx = (t * dtx) * xx, gy = (t * dty) * yy[r], gz = (t * dtz) * zz;
-                    P[g0 + (uint32_t)(r * p.ldz) + po] = to_store<S, T>(((ld<T>(Bp, bi) - gx) - gy) - gz);
+                    const T ta = ((T)rv.x * (T)vv.x) * (T)vv.x, tb = ((T)rv.y * (T)vv.y) * (T)vv.y;
+                    const T pa = ((Po.a - (ta * dtx) * xx.a) - (ta * dty) * yy[r].a) - (ta * dtz) * zz.a;
+                    const T pb = ((Po.b - (tb * dtx) * xx.b) - (tb * dty) * yy[r].b) - (tb * dtz) * zz.b;
+                    st2<S, T>(P, gb[r] + po, pa, pb);
                 }
                 return;
             }
-            const float ay1 = p.ay1[o], ay2 = p.ay2[o];
             const bool yrec = o >= p.npml && o < p.npml + p.ny;
+            // one cell of the general update: damped axes keep split components
+            auto cell = [&](T xx, T yy_, T zz, float rv, float vv, T Po, bool dx, bool dz, float ax1_,
+                            float ax2_, float az1_, float az2_, int bi, uint32_t g, bool store) -> T {
+                T gx, gy, gz;
+                if (!(dx | dym | dz)) {  // a1 == 1 on every axis
+                    const T t = ((T)rv * (T)vv) * (T)vv;
+                    gx = (t * dtx) * xx;
+                    gy = (t * dty) * yy_;
+                    gz = (t * dtz) * zz;
+                    return ((Po - gx) - gy) - gz;
+                }
+                gx = (((((T)ax1_ * (T)rv) * (T)vv) * (T)vv) * dtx) * xx;  // ..iso..:182-184
+                gy = (((((T)ay1 * (T)rv) * (T)vv) * (T)vv) * dty) * yy_;
+                gz = (((((T)az1_ * (T)rv) * (T)vv) * (T)vv) * dtz) * zz;
+                T cx = dx ? ld<T>(Bx, bi) : T(0), cy = dym ? ld<T>(By, bi) : T(0), cz = dz ? ld<T>(Bz, bi) : T(0);
+                const T Pn = pupdate_r<T>(Po, gx, gy, gz, dx, dym, dz, ax2_, ay2, az2_, cx, cy, cz);
+                if (store) {
+                    if (dx) px[g] = to_store<S, T>(cx);
+                    if (dym) py[g] = to_store<S, T>(cy);
+                    if (dz) pz[g] = to_store<S, T>(cz);
+                }
+                return Pn;
+            };
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const int bi = (xw + r) * 32 + tz, cw = (xw + r) * 40 + tz + MM;
-                T xx = 0, zz = 0;
-#pragma unroll
-                for (int im = 0; im < 4; ++im) {  // ..iso..:178-180
-                    xx = fma_t(k[im], us[r + 4 + im] - us[r + 3 - im], xx);
-                    zz = fma_t(k[im], ld<T>(Bw, cw + im) - ld<T>(Bw, cw - im - 1), zz);
-                }
-                const T yr = yy[r];
-                const T rv = (T)Br[bi], vv = (T)Bvp[bi];
-                T gx, gy, gz;
-                const bool dmp = dxm[r] | dym | dzm;
-                if (!dmp) {  // a1 == 1 on every axis: (((1 * rho) * vp) * vp) == (rho * vp) * vp
-                    const T t = (rv * vv) * vv;
-                    gx = (t * dtx) * xx;
-                    gy = (t * dty) * yr;
-                    gz = (t * dtz) * zz;
-                } else {  // ..iso..:182-184
-                    gx = (((((T)ax1[r] * rv) * vv) * vv) * dtx) * xx;
-                    gy = (((((T)ay1 * rv) * vv) * vv) * dty) * yr;
-                    gz = (((((T)az1 * rv) * vv) * vv) * dtz) * zz;
-                }
-                const T Po = ld<T>(Bp, bi);
+                const int bi = (xw + r) * 32 + zl;
+                T2 xx, zz;
+                deriv(r, xx, zz);
+                const float2 rv = *reinterpret_cast<const float2 *>(Br + bi);
+                const float2 vv = *reinterpret_cast<const float2 *>(Bvp + bi);
+                const T2 Po = ld2<T>(Bp, bi);
                 const uint32_t g = gb[r] + po;
-                T Pn;
-                if (!dmp) {
-                    Pn = ((Po - gx) - gy) - gz;
-                } else {
-                    T cx = dxm[r] ? ld<T>(Bx, bi) : T(0), cy = dym ? ld<T>(By, bi) : T(0),
-                      cz = dzm ? ld<T>(Bz, bi) : T(0);
-                    Pn = pupdate_r<T>(Po, gx, gy, gz, dxm[r], dym, dzm, ax2[r], ay2, az2, cx, cy, cz);
-                    if (act[r]) {
-                        if (dxm[r]) px[g] = to_store<S, T>(cx);
-                        if (dym) py[g] = to_store<S, T>(cy);
-                        if (dzm) pz[g] = to_store<S, T>(cz);
-                    }
-                }
-                if (act[r]) P[g] = to_store<S, T>(Pn);
-                if (rec[r] && yrec) {  // ..iso..:294-304
+                const T pa = cell(xx.a, yy[r].a, zz.a, rv.x, vv.x, Po.a, dxm[r], dza, ax1[r], ax2[r], az1.x, az2.x,
+                                  bi, g, act[r]);
+                const T pb = cell(xx.b, yy[r].b, zz.b, rv.y, vv.y, Po.b, dxm[r], dzb, ax1[r], ax2[r], az1.y, az2.y,
+                                  bi + 1, g + 1, act[r] && both);
+                if (act[r]) st2m<S, T>(P, g, pa, pb, both);
+                if (yrec && (reca[r] | recb[r])) {  // ..iso..:294-304
                     const size_t tr = (size_t)trb[r] + (size_t)p.nx * (o - p.npml);
-                    T rr = Pn;
+                    T rr = reca[r] ? pa : pb;
                     if (p.mute_nt && p.it < p.mute_nt[tr]) rr = T(0);
                     p.rec[tr * p.nt + p.it] = (float)rr;
                 }
@@ -388,7 +455,7 @@ __global__ void __launch_bounds__(32 * (TX / R) + 32)
 template <int TX, class S, int D, int R>
 static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
-    constexpr int NT = 32 * (TX / R) + 32;
+    constexpr int NT = 32 * (TX / (2 * R) + 1);
     if (L.kind == K1_ISO_VEL) {
         static bool attr = false;
         Maps<5> mp;
@@ -409,13 +476,19 @@ static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
 // configurations: (tile width, rows per warp) in {8, 16} x {1, 2} and (16, 4), two ring depths
 cudaError_t launch_iso(const K1Launch &L, cudaStream_t st) {
     if (L.fp64) return launch_iso_t<8, double, 0, 2>(L, st);
+    // one of three ring depths for each (tile width, rows per lane) shape
+#define A3D_BY_DEPTH(TX_, R_)                                                   \
+    return L.depth == 2 ? launch_iso_t<TX_, float, 2, R_>(L, st)                \
+         : L.depth == 1 ? launch_iso_t<TX_, float, 1, R_>(L, st)                \
+                        : launch_iso_t<TX_, float, 0, R_>(L, st)
     if (L.tx == 16) {
-        if (L.rows == 4) return L.deep ? launch_iso_t<16, float, 1, 4>(L, st) : launch_iso_t<16, float, 0, 4>(L, st);
-        if (L.rows == 1) return L.deep ? launch_iso_t<16, float, 1, 1>(L, st) : launch_iso_t<16, float, 0, 1>(L, st);
-        return L.deep ? launch_iso_t<16, float, 1, 2>(L, st) : launch_iso_t<16, float, 0, 2>(L, st);
+        if (L.rows == 4) A3D_BY_DEPTH(16, 4);
+        if (L.rows == 1) A3D_BY_DEPTH(16, 1);
+        A3D_BY_DEPTH(16, 2);
     }
-    if (L.rows == 1) return L.deep ? launch_iso_t<8, float, 1, 1>(L, st) : launch_iso_t<8, float, 0, 1>(L, st);
-    return L.deep ? launch_iso_t<8, float, 1, 2>(L, st) : launch_iso_t<8, float, 0, 2>(L, st);
+    if (L.rows == 1) A3D_BY_DEPTH(8, 1);
+    A3D_BY_DEPTH(8, 2);
+#undef A3D_BY_DEPTH
 }
 
 }  // namespace a3d

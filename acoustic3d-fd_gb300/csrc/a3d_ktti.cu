@@ -292,8 +292,8 @@ static cudaError_t launch_tti_t(const K1Launch &L, cudaStream_t st) {
 
 cudaError_t launch_tti(const K1Launch &L, cudaStream_t st) {
     if (L.fp64) return launch_tti_t<8, double, 0>(L, st);
-    if (L.tx == 16) return L.deep ? launch_tti_t<16, float, 1>(L, st) : launch_tti_t<16, float, 0>(L, st);
-    return L.deep ? launch_tti_t<8, float, 1>(L, st) : launch_tti_t<8, float, 0>(L, st);
+    if (L.tx == 16) return L.depth ? launch_tti_t<16, float, 1>(L, st) : launch_tti_t<16, float, 0>(L, st);
+    return L.depth ? launch_tti_t<8, float, 1>(L, st) : launch_tti_t<8, float, 0>(L, st);
 }
 
 }  // namespace a3d

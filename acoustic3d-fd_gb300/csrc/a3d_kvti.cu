@@ -280,8 +280,8 @@ static cudaError_t launch_vti_t(const K1Launch &L, cudaStream_t st) {
 
 cudaError_t launch_vti(const K1Launch &L, cudaStream_t st) {
     if (L.fp64) return launch_vti_t<8, double, 0>(L, st);
-    if (L.tx == 16) return L.deep ? launch_vti_t<16, float, 1>(L, st) : launch_vti_t<16, float, 0>(L, st);
-    return L.deep ? launch_vti_t<8, float, 1>(L, st) : launch_vti_t<8, float, 0>(L, st);
+    if (L.tx == 16) return L.depth ? launch_vti_t<16, float, 1>(L, st) : launch_vti_t<16, float, 0>(L, st);
+    return L.depth ? launch_vti_t<8, float, 1>(L, st) : launch_vti_t<8, float, 0>(L, st);
 }
 
 }  // namespace a3d

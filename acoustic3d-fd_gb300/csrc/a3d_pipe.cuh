@@ -167,28 +167,60 @@ __device__ __forceinline__ void static_for(F &&f) {
 }
 }  // namespace detail
 
-template <int KA, int KB>
+// Ring geometry of the merged pipeline.  A stages have a fixed size; B items are
+// allocated in order from a circular byte ring of RB bytes, each taking only the
+// bytes it needs (items whose tile or plane touches the damped PML carry split
+// components, interior items do not), so more planes fit in flight.
+//   D = 0: 8 A stages, 4 B slots, RB = 4 largest items
+//   D = 1: 16 A stages, 8 B slots, RB = 8 largest items
+//   D = 2: 12 A stages, 12 B slots, RB = what is left of half an SM's shared memory
+//          (two CTAs per SM), the deepest rings two CTAs per SM can hold
+constexpr size_t SMEM_PER_SM = 233472;  // 228 KB per SM (sm_100 family)
+constexpr size_t SMEM_RESERVED_PER_CTA = 1024;
+
+template <int KA_, int KB_>
 struct PipeBarsM {
-    uint64_t full[KA], emptyA[KA], emptyB[KB];
+    uint64_t full[KA_], emptyA[KA_], emptyB[KB_];
+    uint32_t boff[KB_];  // byte offset of the B item in each slot (written by the producer)
+    uint32_t bsz[KB_];   // bytes the item occupies, including wrap-around waste
     int abort_flag;
     __device__ void init(int nconsumers) {  // nconsumers: consumer warps
-        for (int i = 0; i < KA; ++i) { mbar_init(&full[i], 1); mbar_init(&emptyA[i], nconsumers); }
-        for (int i = 0; i < KB; ++i) mbar_init(&emptyB[i], nconsumers);
+        for (int i = 0; i < KA_; ++i) { mbar_init(&full[i], 1); mbar_init(&emptyA[i], nconsumers); }
+        for (int i = 0; i < KB_; ++i) mbar_init(&emptyB[i], nconsumers);
         abort_flag = 0;
         fence_mbar_init();
     }
     __device__ volatile int *abort_ptr() { return &abort_flag; }
 };
 
-// Producer (one thread): issue(sa, sb, bar, seg, q) posts the item's expect_tx on
-// bar and issues its copies: the A copy of plane q into A stage sa and, when
-// sb >= 0, the B copies of plane q-4 into B stage sb.
-template <int TX, int KA, int KB, class Issue>
+template <int D, size_t A_STRIDE, size_t B_MAX>
+struct Ring {
+    static constexpr int KA = D == 0 ? 8 : (D == 1 ? 16 : 12);
+    static constexpr int KB = D == 0 ? 4 : (D == 1 ? 8 : 12);
+    using Bars = PipeBarsM<KA, KB>;
+    static constexpr size_t FIXED = KA * A_STRIDE + (sizeof(Bars) + 127) / 128 * 128;
+    static constexpr size_t BUDGET = SMEM_PER_SM / 2 - SMEM_RESERVED_PER_CTA;
+    static constexpr size_t RB = D == 0 ? 4 * B_MAX
+                               : D == 1 ? 8 * B_MAX
+                                        : (BUDGET > FIXED + B_MAX ? (BUDGET - FIXED) / 128 * 128 : B_MAX);
+    static constexpr size_t B_OFF = KA * A_STRIDE;  // ring B follows the A stages
+    static constexpr size_t BAR_OFF = B_OFF + RB;
+    static constexpr size_t TOTAL = BAR_OFF + sizeof(Bars);
+    static_assert(B_MAX % 128 == 0 && A_STRIDE % 128 == 0, "stages are 128-byte aligned");
+};
+
+// Producer (one thread): for every item, bsize(seg, o) gives the bytes of the B
+// part of output plane o (a multiple of 128), the ring allocates them, and
+// issue(sa, bdst, bbytes, bar, seg, q) posts the item's expect_tx on bar and
+// issues its copies: the A copy of plane q into A stage sa and, when bdst is not
+// null, the B copies of plane q-4 into bdst.
+template <int TX, int KA, int KB, size_t RB, class BSize, class Issue>
 __device__ __forceinline__ void pipe_produce_m(const Sweep &sw, long long w0, long long w1,
-                                               PipeBarsM<KA, KB> &b, int *err, Issue issue) {
-    static_assert((KA & (KA - 1)) == 0 && (KB & (KB - 1)) == 0, "ring sizes are powers of two");
+                                               PipeBarsM<KA, KB> &b, unsigned char *ringB, int *err,
+                                               BSize bsize, Issue issue) {
     volatile int *ab = b.abort_ptr();
     uint32_t ja = 0, jb = 0;
+    uint32_t head = 0, used = 0, tail = 0;  // B ring: next free byte, bytes held, oldest live item
     bool ok = true;
     for (long long w = w0; w < w1 && ok;) {
         long long wend;
@@ -197,15 +229,36 @@ __device__ __forceinline__ void pipe_produce_m(const Sweep &sw, long long w0, lo
             const uint32_t sa = ja % KA;
             if (ja >= KA && !(ok = mbar_wait(&b.emptyA[sa], ((ja / KA) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab)))
                 break;
-            int sb = -1;
+            unsigned char *bdst = nullptr;
+            uint32_t sz = 0;
             if (q - MM >= s.ya) {
-                sb = (int)(jb % KB);
-                if (jb >= KB &&
-                    !(ok = mbar_wait(&b.emptyB[sb], ((jb / KB) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab)))
-                    break;
+                sz = bsize(s, q - MM);
+                for (;;) {
+                    if (tail == jb) head = used = 0;  // ring empty: start over at byte 0
+                    uint32_t off = head, waste = 0;
+                    if (off + sz > RB) {
+                        waste = (uint32_t)RB - off;
+                        off = 0;
+                    }
+                    if (jb - tail < (uint32_t)KB && used + waste + sz <= (uint32_t)RB) {
+                        const uint32_t slot = jb % KB;
+                        b.boff[slot] = off;
+                        b.bsz[slot] = waste + sz;
+                        used += waste + sz;
+                        head = off + sz;
+                        bdst = ringB + off;
+                        break;
+                    }
+                    // wait for the consumers to release the oldest live item
+                    if (!(ok = mbar_wait(&b.emptyB[tail % KB], (tail / KB) & 1, err, KERR_EMPTY_TIMEOUT, ab)))
+                        break;
+                    used -= b.bsz[tail % KB];
+                    ++tail;
+                }
+                if (!ok) break;
                 ++jb;
             }
-            issue(sa, sb, &b.full[sa], s, q);
+            issue(sa, bdst, sz, &b.full[sa], s, q);
             ++ja;
         }
         w = wend;
@@ -235,14 +288,14 @@ __device__ __forceinline__ void with_phase(int ph, F &&f) {
 //   onSeg(seg)                         at a segment start
 //   fill(ph, sa, seg, q)               planes q = ya-4 .. ya+3 (window fill); ph = item
 //                                      index in the segment (= q - ya + 4), a constant
-//   step(ph, sa, sh, sb, seg, q)       planes q >= ya+4: A stage sa (plane q), A stage sh
-//                                      (plane q-HOLD), B stage sb (output plane q-4);
+//   step(ph, sa, sh, bp, seg, q)       planes q >= ya+4: A stage sa (plane q), A stage sh
+//                                      (plane q-HOLD), the B item of output plane q-4 at bp;
 //                                      ph = item index mod 8 (run time: see with_phase)
 // Returns false on abort.
 template <int TX, int KA, int KB, int HOLD, class OnSeg, class Fill, class Step>
 __device__ __forceinline__ bool pipe_run(const Sweep &sw, long long w0, long long w1,
-                                         PipeBarsM<KA, KB> &b, int *err, OnSeg onSeg, Fill fill,
-                                         Step step) {
+                                         PipeBarsM<KA, KB> &b, const unsigned char *ringB, int *err,
+                                         OnSeg onSeg, Fill fill, Step step) {
     static_assert(HOLD == 0 || HOLD == MM, "A stages are held 0 or 4 items");
     volatile int *ab = b.abort_ptr();
     const bool lead = (threadIdx.x & 31) == 0;
@@ -266,7 +319,7 @@ __device__ __forceinline__ bool pipe_run(const Sweep &sw, long long w0, long lon
         for (int q = s.ya + MM; q < qe; ++q) {
             const uint32_t sa = ja % KA, sh = (ja - HOLD) % KA, sb = jb % KB;
             if (!mbar_wait(&b.full[sa], (ja / KA) & 1, err, KERR_FULL_TIMEOUT, ab)) return false;
-            step(q - s.ya + MM, sa, sh, sb, s, q);
+            step(q - s.ya + MM, sa, sh, ringB + b.boff[sb], s, q);
             __syncwarp();
             if (lead) {
                 mbar_arrive(&b.emptyB[sb]);
