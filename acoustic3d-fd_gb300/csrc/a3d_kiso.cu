@@ -404,28 +404,30 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 return;
             }
             const bool yrec = o >= p.npml && o < p.npml + p.ny;
-            // one cell of the general update: damped axes keep split components
-            auto cell = [&](T xx, T yy_, T zz, float rv, float vv, T Po, bool dx, bool dz, float ax1_,
-                            float ax2_, float az1_, float az2_, int bi, uint32_t g, bool store) -> T {
-                T gx, gy, gz;
-                if (!(dx | dym | dz)) {  // a1 == 1 on every axis
-                    const T t = ((T)rv * (T)vv) * (T)vv;
-                    gx = (t * dtx) * xx;
-                    gy = (t * dty) * yy_;
-                    gz = (t * dtz) * zz;
-                    return ((Po - gx) - gy) - gz;
-                }
-                gx = (((((T)ax1_ * (T)rv) * (T)vv) * (T)vv) * dtx) * xx;  // ..iso..:182-184
-                gy = (((((T)ay1 * (T)rv) * (T)vv) * (T)vv) * dty) * yy_;
-                gz = (((((T)az1_ * (T)rv) * (T)vv) * (T)vv) * dtz) * zz;
-                T cx = dx ? ld<T>(Bx, bi) : T(0), cy = dym ? ld<T>(By, bi) : T(0), cz = dz ? ld<T>(Bz, bi) : T(0);
-                const T Pn = pupdate_r<T>(Po, gx, gy, gz, dx, dym, dz, ax2_, ay2, az2_, cx, cy, cz);
-                if (store) {
-                    if (dx) px[g] = to_store<S, T>(cx);
-                    if (dym) py[g] = to_store<S, T>(cy);
-                    if (dz) pz[g] = to_store<S, T>(cz);
-                }
-                return Pn;
+            // General update (tiles or planes on a damped axis), the oracle's engine form
+            // (engine_pupdate) for both cells of the lane without branches: a damped axis
+            // keeps its split component, an undamped one subtracts its term directly; the
+            // selects keep the operation order, so undamped cells get ((P - gx) - gy) - gz.
+            // a1 == 1 off the PML, so one product chain serves every cell (..iso..:182-184).
+            auto upd = [&](T Po, T xx, T yy_, T zz, float rv, float vv, bool dx, bool dz, float ax1_, float ax2_,
+                           float az1_, float az2_, T cx, T cy, T cz, T &nx, T &ny, T &nz) -> T {
+                const T gx = (((((T)ax1_ * (T)rv) * (T)vv) * (T)vv) * dtx) * xx;
+                const T gy = (((((T)ay1 * (T)rv) * (T)vv) * (T)vv) * dty) * yy_;
+                const T gz = (((((T)az1_ * (T)rv) * (T)vv) * (T)vv) * dtz) * zz;
+                T q = Po;
+                q = dx ? q - cx : q;
+                q = dym ? q - cy : q;
+                q = dz ? q - cz : q;
+                q = dx ? q : q - gx;
+                q = dym ? q : q - gy;
+                q = dz ? q : q - gz;
+                nx = fma_t((T)ax2_, cx, -gx);
+                ny = fma_t((T)ay2, cy, -gy);
+                nz = fma_t((T)az2_, cz, -gz);
+                q = dx ? q + nx : q;
+                q = dym ? q + ny : q;
+                q = dz ? q + nz : q;
+                return q;
             };
 #pragma unroll
             for (int r = 0; r < R; ++r) {
@@ -435,12 +437,27 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 const float2 rv = *reinterpret_cast<const float2 *>(Br + bi);
                 const float2 vv = *reinterpret_cast<const float2 *>(Bvp + bi);
                 const T2 Po = ld2<T>(Bp, bi);
+                // split components present in this item (tile- and plane-level flags)
+                const T2 cx = tdx ? ld2<T>(Bx, bi) : T2{0, 0};
+                const T2 cy = dym ? ld2<T>(By, bi) : T2{0, 0};
+                const T2 cz = tdz ? ld2<T>(Bz, bi) : T2{0, 0};
                 const uint32_t g = gb[r] + po;
-                const T pa = cell(xx.a, yy[r].a, zz.a, rv.x, vv.x, Po.a, dxm[r], dza, ax1[r], ax2[r], az1.x, az2.x,
-                                  bi, g, act[r]);
-                const T pb = cell(xx.b, yy[r].b, zz.b, rv.y, vv.y, Po.b, dxm[r], dzb, ax1[r], ax2[r], az1.y, az2.y,
-                                  bi + 1, g + 1, act[r] && both);
-                if (act[r]) st2m<S, T>(P, g, pa, pb, both);
+                T nxa, nya, nza, nxb, nyb, nzb;
+                const T pa = upd(Po.a, xx.a, yy[r].a, zz.a, rv.x, vv.x, dxm[r], dza, ax1[r], ax2[r], az1.x, az2.x,
+                                 cx.a, cy.a, cz.a, nxa, nya, nza);
+                const T pb = upd(Po.b, xx.b, yy[r].b, zz.b, rv.y, vv.y, dxm[r], dzb, ax1[r], ax2[r], az1.y, az2.y,
+                                 cx.b, cy.b, cz.b, nxb, nyb, nzb);
+                if (act[r]) {
+                    st2m<S, T>(P, g, pa, pb, both);
+                    if (dxm[r]) st2m<S, T>(px, g, nxa, nxb, both);
+                    if (dym) st2m<S, T>(py, g, nya, nyb, both);
+                    if (dza && dzb && both) {
+                        st2<S, T>(pz, g, nza, nzb);
+                    } else {
+                        if (dza) pz[g] = to_store<S, T>(nza);
+                        if (dzb && both) pz[g + 1] = to_store<S, T>(nzb);
+                    }
+                }
                 if (yrec && (reca[r] | recb[r])) {  // ..iso..:294-304
                     const size_t tr = (size_t)trb[r] + (size_t)p.nx * (o - p.npml);
                     T rr = reca[r] ? pa : pb;
