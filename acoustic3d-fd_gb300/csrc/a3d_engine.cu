@@ -3,6 +3,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstdarg>
@@ -73,29 +74,38 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 3-D map over a padded field: dims (nnz, nnx, nny), row stride ldz elements
-static int make_map(CUtensorMap *m, const void *base, bool f64, const Grid &g, int box0, int box1) {
+// 3-D map over a padded field: dims (nnz, nnx, nny), row stride ldz elements.
+// dtype: 0 float, 1 bfloat16, 2 float16, 3 double.  A 2-byte field's base (the
+// allocation + zoff elements) is only 8-byte aligned, so its map starts 4 elements
+// earlier (16-byte aligned) and kernels add 4 to its z coordinates.
+static int make_map(CUtensorMap *m, const void *base, int dtype, const Grid &g, int box0, int box1) {
     auto enc = encode_fn();
     if (!enc) return fail(A3D_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
-    const size_t es = f64 ? 8 : 4;
-    cuuint64_t dims[3] = {(cuuint64_t)g.nnz, (cuuint64_t)g.nnx, (cuuint64_t)g.nny};
+    const size_t es = dtype == 3 ? 8 : (dtype == 0 ? 4 : 2);
+    const int zs = es == 2 ? 4 : 0;
+    const char *b = static_cast<const char *>(base) - zs * es;
+    cuuint64_t dims[3] = {(cuuint64_t)(g.nnz + zs), (cuuint64_t)g.nnx, (cuuint64_t)g.nny};
     cuuint64_t strides[2] = {(cuuint64_t)(g.ldz * es), (cuuint64_t)((size_t)g.ldz * g.nnx * es)};
     cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, 1};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = enc(m, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
-                     const_cast<void *>(base), dims, strides, box, estr,
+    const CUtensorMapDataType dt = dtype == 3   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                   : dtype == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                   : dtype == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    CUresult r = enc(m, dt, 3, const_cast<char *>(b), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                      CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(A3D_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return A3D_OK;
 }
 
-int make_field_map(CUtensorMap *m, const void *base, bool f64, const Grid &g, int box0, int box1) {
-    return make_map(m, base, f64, g, box0, box1);
+int make_field_map(CUtensorMap *m, const void *base, int dtype, const Grid &g, int box0, int box1) {
+    return make_map(m, base, dtype, g, box0, box1);
 }
 
-static int box_dims(int box, int tx, int &b0, int &b1) {
-    b0 = (box == BOX_HZ || box == BOX_H) ? 40 : 32;
+// zhalo: width of z-halo'd boxes (40, or 48 for 2-byte storage: see ZHalo)
+static int box_dims(int box, int tx, int &b0, int &b1, int zhalo = 40) {
+    b0 = (box == BOX_HZ || box == BOX_H) ? zhalo : 32;
     b1 = (box == BOX_HX || box == BOX_H) ? tx + 8 : tx;
     return 0;
 }
@@ -103,14 +113,14 @@ static int box_dims(int box, int tx, int &b0, int &b1) {
 // crop of the model window of a padded field into dense float [ny][nx][nz]
 template <class S>
 __global__ void crop_window(const S *f, float *out, int nx, int ny, int nz, int pad, int ldz,
-                            int nnx) {
+                            int nnx, float scale) {
     const size_t n = (size_t)nx * ny * nz;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x) {
         const int iz = (int)(i % nz);
         const size_t r = i / nz;
         const int ix = (int)(r % nx), iy = (int)(r / nx);
-        out[i] = (float)f[(size_t)(iz + pad) + (size_t)ldz * ((size_t)(ix + pad) + (size_t)nnx * (iy + pad))];
+        out[i] = (float)f[(size_t)(iz + pad) + (size_t)ldz * ((size_t)(ix + pad) + (size_t)nnx * (iy + pad))] * scale;
     }
 }
 
@@ -198,10 +208,10 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
         for (int t = 0; t < 2; ++t) {
             const int tx = t ? 16 : 8;
             for (int b = 0; b < 2; ++b) {
-                if ((rc = make_map(&e->m2o_cur[t][b], buf[b], f64, g, 40, tx + 8))) return rc;
-                if ((rc = make_map(&e->m2o_prev[t][b], buf[b], f64, g, 32, tx))) return rc;
+                if ((rc = make_map(&e->m2o_cur[t][b], buf[b], f64 ? 3 : 0, g, 40, tx + 8))) return rc;
+                if ((rc = make_map(&e->m2o_prev[t][b], buf[b], f64 ? 3 : 0, g, 32, tx))) return rc;
             }
-            if ((rc = make_map(&e->m2o_vv[t], e->vv, false, g, 32, tx))) return rc;
+            if ((rc = make_map(&e->m2o_vv[t], e->vv, 0, g, 32, tx))) return rc;
         }
         return A3D_OK;
     }
@@ -298,6 +308,23 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
             e->amp1[it] = pfac * src;
         }
     }
+    // float16 storage scales (powers of two, so every rescaling is exact): P so that
+    // the largest injected amplitude maps to 2^11 (headroom to the float16 maximum
+    // 65504); u, v, w by the velocity-to-pressure ratio dx rho / dt on top of that,
+    // so that both kinds of field sit in the same part of the float16 range.
+    // bfloat16 keeps float's exponent range and needs no scaling.
+    if (e->half == 2 && rho) {
+        float amax = 0.0f;
+        for (int it = 0; it < c.nt; ++it)
+            if (e->inj[it]) amax = std::max(amax, std::max(std::fabs(e->amp0[it]), std::fabs(e->amp1[it])));
+        double rsum = 0.0;
+        const size_t n = (size_t)c.nx * c.ny * c.nz;
+        for (size_t i = 0; i < n; ++i) rsum += rho[i];
+        const double rmean = rsum / (double)n;
+        const double dmin = std::min(c.dx, std::min(c.dy, c.dz));
+        if (amax > 0.0f) e->sig_p = std::ldexp(1.0f, (int)std::floor(std::log2(2048.0 / amax)));
+        e->sig_v = e->sig_p * std::ldexp(1.0f, (int)std::lround(std::log2(dmin * rmean / c.dt)));
+    }
     // tensor maps for both tile widths
     const bool f64 = e->fp64;
     for (int t = 0; t < 2; ++t) {
@@ -305,8 +332,8 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     CUtensorMap *mvel = e->mvel[t], *mstr = e->mstr[t];
     int b0, b1;
     auto mk = [&](CUtensorMap *m, const void *p, bool isfield, int box) {
-        box_dims(box, tx, b0, b1);
-        return make_map(m, p, isfield && f64, g, b0, b1);
+        box_dims(box, tx, b0, b1, isfield && e->half ? 48 : 40);
+        return make_map(m, p, isfield ? (f64 ? 3 : e->half) : 0, g, b0, b1);
     };
     if (c.physics == A3D_ISO) {
         e->nvel = 5;
@@ -461,6 +488,8 @@ int a3d_engine::autotune() {
                 L.nmaps = k == 0 ? nvel : nstr;
                 L.out0 = k == 0 ? u : P; L.out1 = k == 0 ? v : Q; L.out2 = w;
                 L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
+                L.half = half;
+                p.svp = p.spv = p.rec_scale = 1.0f;
                 auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
                 return launch(L, st);
             };
@@ -509,10 +538,15 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
     auto snapshot = [&](int it, const void *field) -> int {
         if (!hook || !hook->want || !hook->want(it)) return A3D_OK;
         const int pad = g.pad;
+        const float sc = 1.0f / sig_p;  // exact: sig_p is a power of two
         if (fp64)
-            crop_window<double><<<1024, 256, 0, st>>>((const double *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx);
+            crop_window<double><<<1024, 256, 0, st>>>((const double *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
+        else if (half == 1)
+            crop_window<__nv_bfloat16><<<1024, 256, 0, st>>>((const __nv_bfloat16 *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
+        else if (half == 2)
+            crop_window<__half><<<1024, 256, 0, st>>>((const __half *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
         else
-            crop_window<float><<<1024, 256, 0, st>>>((const float *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx);
+            crop_window<float><<<1024, 256, 0, st>>>((const float *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
         CUDA_TRY(cudaGetLastError());
         snap_host.resize((size_t)c.nx * c.ny * c.nz);
         CUDA_TRY(cudaMemcpyAsync(snap_host.data(), snap_dev, snap_host.size() * 4, cudaMemcpyDeviceToHost, st));
@@ -629,6 +663,9 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         p.mute_nt = c.mute ? d_mute : nullptr;
         p.nt = c.nt;
         p.err = d_err;
+        p.svp = sig_v / sig_p;  // powers of two: exact
+        p.spv = sig_p / sig_v;
+        p.rec_scale = 1.0f / sig_p;
         const int kv = c.physics == A3D_ISO ? K1_ISO_VEL : (c.physics == A3D_VTI ? K1_VTI_VEL : K1_TTI_VEL);
         Lv.kind = kv; Ls.kind = kv + 1;
         Lv.maps = mvel[tune[0].tx == 16 ? 1 : 0]; Lv.nmaps = nvel;
@@ -637,15 +674,15 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         Ls.out0 = P; Ls.out1 = Q;
         Lv.tx = tune[0].tx; Lv.depth = tune[0].depth; Lv.mode = tune[0].mode; Lv.rows = tune[0].rows;
         Ls.tx = tune[1].tx; Ls.depth = tune[1].depth; Ls.mode = tune[1].mode; Ls.rows = tune[1].rows;
-        Lv.fp64 = Ls.fp64 = fp64; Lv.grid = Ls.grid = 0;
+        Lv.fp64 = Ls.fp64 = fp64; Lv.half = Ls.half = half; Lv.grid = Ls.grid = 0;
         auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
         if ((rc = prepare_profiling(this, 3))) return rc;
         rc = time_loop([&]() -> int {
             for (int it = 0; it < c.nt; ++it) {
                 p.it = it;
                 p.inj = inj[it];
-                p.amp0 = amp0[it];
-                p.amp1 = amp1[it];
+                p.amp0 = amp0[it] * sig_p;  // exact: sig_p is a power of two
+                p.amp1 = amp1[it] * sig_p;
                 Lv.p = p;
                 Ls.p = p;
                 if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it], st));
@@ -689,7 +726,8 @@ static int validate(const a3d_config *c) {
         return fail(A3D_E_ARG, "grid %dx%dx%d, nt %d must be positive", c->nx, c->ny, c->nz, c->nt);
     if (!(c->dx > 0) || !(c->dy > 0) || !(c->dz > 0) || !(c->dt > 0) || !(c->fm > 0))
         return fail(A3D_E_ARG, "dx, dy, dz, dt and fm must be positive");
-    if (c->storage != A3D_FP32 && c->storage != A3D_FP64)
+    if (c->storage != A3D_FP32 && c->storage != A3D_FP64 &&
+        !((c->storage == A3D_BF16 || c->storage == A3D_FP16) && c->physics == A3D_ISO))
         return fail(A3D_E_UNSUPPORTED, "storage type %d is not built for this engine", c->storage);
     if (c->physics == A3D_ISO && (c->wtype < 1 || c->wtype > 6))
         return fail(A3D_E_ARG, "wavelet type %d outside 1..6", c->wtype);
@@ -718,7 +756,8 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
     e->cfg = *cfg;
     e->device = device;
     e->fp64 = cfg->storage == A3D_FP64;
-    e->esz = e->fp64 ? 8 : 4;
+    e->half = cfg->storage == A3D_BF16 ? 1 : (cfg->storage == A3D_FP16 ? 2 : 0);
+    e->esz = e->fp64 ? 8 : (e->half ? 2 : 4);
     e->tx = 8;
     if (ph == A3D_2ORDER) {
         e->npml = cfg->npml > 0 ? cfg->npml : 50;  // npd, 2O:19

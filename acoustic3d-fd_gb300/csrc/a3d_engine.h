@@ -15,7 +15,8 @@ int fail(int code, const char *fmt, ...);
 void clear_error();
 
 // tensor map over a padded field (dims nnz, nnx, nny; rows of g.ldz elements)
-int make_field_map(CUtensorMap *m, const void *base, bool f64, const Grid &g, int box0, int box1);
+// dtype: 0 float, 1 bfloat16, 2 float16, 3 double
+int make_field_map(CUtensorMap *m, const void *base, int dtype, const Grid &g, int box0, int box1);
 
 // snapshot hook: want(it) says whether a snapshot is taken after step it;
 // take(it, window) receives the model window (nz*nx*ny floats, z fastest)
@@ -33,7 +34,11 @@ struct a3d_engine {
     int npml = 0;          // absorber cells (1st order) or sponge width npd (2nd order)
     int tx = 8;
     bool fp64 = false;
+    int half = 0;          // 2-byte wavefields: 1 bfloat16, 2 float16 (isotropic engine)
     size_t esz = 4;        // bytes per wavefield element
+    // power-of-two storage scales of 2-byte wavefields: sig_v for u, v, w, sig_p for P
+    // and its split components (1 otherwise)
+    float sig_v = 1.0f, sig_p = 1.0f;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int *d_err = nullptr;

@@ -26,6 +26,12 @@ struct K1Params {
     const int *mute_nt;
     int it, nt;
     int *err;
+    // 2-byte storage: fields hold sigma * value with power-of-two scales (sigma_v for
+    // u, v, w; sigma_P for P and its split components), so scaling is exact and is
+    // folded into coefficients: svp = sigma_v / sigma_P multiplies the velocity
+    // terms, spv = sigma_P / sigma_v the pressure terms, rec_scale = 1 / sigma_P
+    // the recorded P.  All 1 for 4- and 8-byte storage.
+    float svp, spv, rec_scale;
 };
 
 enum K1Kind { K1_ISO_VEL = 0, K1_ISO_STR, K1_VTI_VEL, K1_VTI_STR, K1_TTI_VEL, K1_TTI_STR };
@@ -41,6 +47,7 @@ struct K1Launch {
     K1Params p;
     int tx, grid;
     bool fp64;
+    int half;   // 2-byte wavefield storage: 0 none, 1 bfloat16, 2 float16
     int depth;  // TMA ring depth (0, 1, 2: see Ring in a3d_pipe.cuh; VTI/TTI: 0, 1)
     int mode;   // sweep plan (plan_sweep)
     int rows;   // tile rows per consumer warp (iso: 2 or 4; VTI/TTI: 1)

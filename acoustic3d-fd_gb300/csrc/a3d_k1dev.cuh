@@ -93,20 +93,51 @@ static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid,
 // loads of a stored field value / smem tile element as the arithmetic type
 template <class T, class S> __device__ __forceinline__ T ld(const S *a, int i) { return from_store<T, S>(a[i]); }
 
+// Wavefield tensor maps of 2-byte storage start 4 elements before the field base
+// (the field base is only 8-byte aligned; base - 4 elements is 16-byte aligned), so
+// their z coordinates are shifted by 4.  That puts both the core box start z0 and
+// the halo box start z0 - 4 on 16-byte boundaries.
+template <class S> struct WFieldZShift { static constexpr int v = sizeof(S) == 2 ? 4 : 0; };
+// Halo'd-in-z wavefield boxes: 4-, 8-byte storage load 40 cells from z0 - 4; with
+// 2-byte storage z0 - 4 and z0 cannot both be 16-byte aligned (they are 8 bytes
+// apart), so those boxes load 48 cells from z0 - 8, which is aligned whenever the
+// core box start z0 is.  ZH = offset of the tile's first z cell inside a halo'd row.
+template <class S> struct ZHalo {
+    static constexpr int ZH = sizeof(S) == 2 ? 8 : 4;
+    static constexpr int W = 32 + 2 * ZH;
+};
+
+// exact power-of-two rescaling of a value for 2-byte storage; identity otherwise
+template <class S, class T> __device__ __forceinline__ T scl(T x, float f) {
+    if constexpr (sizeof(S) == 2) return x * (T)f;
+    else return x;
+}
+
 // Two z-adjacent cells per lane: elements i, i+1 (i even, so the pair is aligned)
 // move as one 8-byte (float) or 16-byte (double) access.
 template <class T> struct Two { T a, b; };
 template <class S> struct Vec2;
 template <> struct Vec2<float> { using t = float2; };
 template <> struct Vec2<double> { using t = double2; };
+template <> struct Vec2<__nv_bfloat16> { using t = __nv_bfloat162; };
+template <> struct Vec2<__half> { using t = __half2; };
+__device__ __forceinline__ float2 to_f2(float2 v) { return v; }
+__device__ __forceinline__ double2 to_f2(double2 v) { return v; }
+__device__ __forceinline__ float2 to_f2(__nv_bfloat162 v) { return __bfloat1622float2(v); }
+__device__ __forceinline__ float2 to_f2(__half2 v) { return __half22float2(v); }
 template <class T, class S> __device__ __forceinline__ Two<T> ld2(const S *p, int i) {
-    const auto v = *reinterpret_cast<const typename Vec2<S>::t *>(p + i);
+    const auto v = to_f2(*reinterpret_cast<const typename Vec2<S>::t *>(p + i));
     return Two<T>{(T)v.x, (T)v.y};
 }
 template <class S, class T> __device__ __forceinline__ void st2(S *p, uint32_t i, T a, T b) {
     typename Vec2<S>::t v;
-    v.x = to_store<S, T>(a);
-    v.y = to_store<S, T>(b);
+    if constexpr (sizeof(S) == 2) {  // round to nearest, as the scalar conversions
+        v.x = to_store<S, float>((float)a);
+        v.y = to_store<S, float>((float)b);
+    } else {
+        v.x = to_store<S, T>(a);
+        v.y = to_store<S, T>(b);
+    }
     *reinterpret_cast<typename Vec2<S>::t *>(p + i) = v;
 }
 // store the pair, or only its first element when the second lies past the sweep

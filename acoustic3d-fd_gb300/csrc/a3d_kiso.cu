@@ -21,7 +21,7 @@ namespace a3d {
 // iso_vel: maps {P (box H), u, v, w (core), 1/rho (core, float)}
 template <int TX, class S, int D>
 struct IsoVelL {
-    static constexpr int AW = 40, AH = TX + 8;
+    static constexpr int AW = ZHalo<S>::W, AH = TX + 8;  // P tile: [AH][AW], z halo ZH
     static constexpr uint32_t A_BYTES = AW * AH * sizeof(S);
     static constexpr uint32_t C = 32 * TX;  // core elements
     static constexpr uint32_t B_BYTES = 3 * C * sizeof(S) + C * 4;
@@ -41,6 +41,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     using T = typename Arith<S>::T;
     using T2 = Two<T>;
     constexpr int NW = TX / (2 * R), NC = 32 * NW, AW = L::AW;
+    constexpr int ZS = WFieldZShift<S>::v;  // z offset of wavefield maps (2-byte storage)
+    constexpr int ZH = ZHalo<S>::ZH;        // first z cell of the tile inside a P row
     static_assert(NW >= 1, "a warp covers 2R tile rows");
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<typename L::Bars *>(smem + L::BAR_OFF);
@@ -59,12 +61,12 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             p.sw, w0, w1, bars, ringB, p.err, [](const Seg &, int) { return (uint32_t)L::B_STRIDE; },
             [&](uint32_t sa, unsigned char *dst, uint32_t, uint64_t *bar, const Seg &s, int q) {
                 mbar_arrive_expect_tx(bar, L::A_BYTES + (dst ? L::B_BYTES : 0u));
-                tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0 - MM, s.x0 - MM, q);
+                tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0 - ZH + ZS, s.x0 - MM, q);
                 if (!dst) return;
                 const int o = q - MM;
-                tma_load_3d(dst, &mp.m[1], bar, s.z0, s.x0, o);
-                tma_load_3d(dst + L::C * sizeof(S), &mp.m[2], bar, s.z0, s.x0, o);
-                tma_load_3d(dst + 2 * L::C * sizeof(S), &mp.m[3], bar, s.z0, s.x0, o);
+                tma_load_3d(dst, &mp.m[1], bar, s.z0 + ZS, s.x0, o);
+                tma_load_3d(dst + L::C * sizeof(S), &mp.m[2], bar, s.z0 + ZS, s.x0, o);
+                tma_load_3d(dst + 2 * L::C * sizeof(S), &mp.m[3], bar, s.z0 + ZS, s.x0, o);
                 tma_load_3d(dst + 3 * L::C * sizeof(S), &mp.m[4], bar, s.z0, s.x0, o);
             });
         return;
@@ -73,7 +75,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     // lane: z cells zl, zl+1 of the tile (zl = 2 (lane mod 16)) in tile rows
     // xw .. xw+R-1, where the two half-warps take consecutive groups of R rows
     const int zl = 2 * (lane & 15), xw = warp * 2 * R + (lane >> 4) * R;
-    const int c0 = (xw + MM) * AW + zl + MM;  // this lane's first cell pair in an A tile
+    const int c0 = (xw + MM) * AW + zl + ZH;  // this lane's first cell pair in an A tile
     T2 win[R][8];                             // P at the last 8 planes, slot = item mod 8
     bool act[R], both = true;
     T cx1d[R], cx2[R];
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     // source plane in place (it serves the window push and, 4 planes later, the
     // in-plane neighbours), then make the write visible to every consumer warp
     auto inject = [&](S *A, const Seg &s) {
-        const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - MM);
+        const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - ZH);
         if (threadIdx.x == 0) {
             if (lz >= 0 && lz < AW) A[lx * AW + lz] = to_store<S, T>(ld<T>(A, lx * AW + lz) + (T)p.amp0);
             if (lz + 2 >= 0 && lz + 2 < AW)
@@ -105,18 +107,18 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             const bool zact = iz < p.nnz - MM;
             both = iz + 1 < p.nnz - MM;
             const int cza = min(iz, p.nnz - 1), czb = min(iz + 1, p.nnz - 1);
-            cz1d = T2{(T)p.cz1[cza] * (T)p.dtz, (T)p.cz1[czb] * (T)p.dtz};
+            cz1d = T2{scl<S>((T)p.cz1[cza] * (T)p.dtz, p.svp), scl<S>((T)p.cz1[czb] * (T)p.dtz, p.svp)};
             cz2 = T2{(T)p.cz2[cza], (T)p.cz2[czb]};
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int ix = s.x0 + xw + r;
                 act[r] = zact && ix < p.nnx - MM;
                 const int cxi = min(ix, p.nnx - 1);
-                cx1d[r] = (T)p.cx1[cxi] * (T)p.dtx;
+                cx1d[r] = scl<S>((T)p.cx1[cxi] * (T)p.dtx, p.svp);
                 cx2[r] = (T)p.cx2[cxi];
                 gb[r] = (uint32_t)iz + (uint32_t)p.ldz * (uint32_t)cxi;
             }
-            const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - MM);
+            const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - ZH);
             srcq = (p.inj && lx >= 0 && lx < L::AH && lz + 2 >= 0 && lz < AW) ? p.s_y : INT_MIN;
             cy1n = p.cy1[s.ya];
             cy2n = p.cy2[s.ya];
@@ -158,7 +160,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             T2 xs[R + 7];
 #pragma unroll
             for (int j = 0; j < R + 7; ++j) xs[j] = ld2<T>(Ao, c0 + (j + 1 - MM) * AW);
-            const T cy1d = (T)cy1n * (T)p.dty, cy2 = (T)cy2n;
+            const T cy1d = scl<S>((T)cy1n * (T)p.dty, p.svp), cy2 = (T)cy2n;
             cy1n = p.cy1[o + 1];  // o + 1 <= nny - 4: in bounds
             cy2n = p.cy2[o + 1];
             const uint32_t po = pstride * (uint32_t)o;
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
 template <int TX, class S, int D>
 struct IsoStrL {
     static constexpr uint32_t C = 32 * TX;
-    static constexpr uint32_t UX = 32 * (TX + 8), WZ = 40 * TX;
+    static constexpr uint32_t UX = 32 * (TX + 8), WZ = ZHalo<S>::W * TX;  // w tile: [TX][W], z halo ZH
     static constexpr uint32_t A_BYTES = C * sizeof(S);
     // fixed part of a B item (u, w, P, rho, vp), then one tile per damped axis
     static constexpr uint32_t B_FIXED = (UX + WZ + C) * sizeof(S) + 2 * C * 4;
@@ -229,6 +231,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     using T = typename Arith<S>::T;
     using T2 = Two<T>;
     constexpr int NW = TX / (2 * R);
+    constexpr int ZS = WFieldZShift<S>::v;  // z offset of wavefield maps (2-byte storage)
     static_assert(NW >= 1, "a warp covers 2R tile rows");
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<typename L::Bars *>(smem + L::BAR_OFF);
@@ -258,18 +261,19 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             p.sw, w0, w1, bars, ringB, p.err, [&](const Seg &s, int o) { return L::B_FIXED + AUX * naux(s, o); },
             [&](uint32_t sa, unsigned char *dst, uint32_t bbytes, uint64_t *bar, const Seg &s, int q) {
                 mbar_arrive_expect_tx(bar, L::A_BYTES + bbytes);
-                tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0, s.x0, q);
+                tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0 + ZS, s.x0, q);
                 if (!dst) return;
                 const int o = q - MM;
-                tma_load_3d(dst, &mp.m[1], bar, s.z0, s.x0 - MM, o);
-                tma_load_3d(dst + oW, &mp.m[2], bar, s.z0 - MM, s.x0, o);
-                tma_load_3d(dst + oP, &mp.m[3], bar, s.z0, s.x0, o);
+                tma_load_3d(dst, &mp.m[1], bar, s.z0 + ZS, s.x0 - MM, o);
+                tma_load_3d(dst + oW, &mp.m[2], bar, s.z0 - ZHalo<S>::ZH + ZS, s.x0, o);
+                tma_load_3d(dst + oP, &mp.m[3], bar, s.z0 + ZS, s.x0, o);
                 tma_load_3d(dst + oR, &mp.m[4], bar, s.z0, s.x0, o);
                 tma_load_3d(dst + oV, &mp.m[5], bar, s.z0, s.x0, o);
                 unsigned char *ax = dst + oX;
-                if (range_damped(s.x0, TX, p.ulo[0], p.uhi[0])) { tma_load_3d(ax, &mp.m[6], bar, s.z0, s.x0, o); ax += AUX; }
-                if (range_damped(o, 1, p.ulo[1], p.uhi[1])) { tma_load_3d(ax, &mp.m[7], bar, s.z0, s.x0, o); ax += AUX; }
-                if (range_damped(s.z0, 32, p.ulo[2], p.uhi[2])) tma_load_3d(ax, &mp.m[8], bar, s.z0, s.x0, o);
+                const int zs = s.z0 + ZS;
+                if (range_damped(s.x0, TX, p.ulo[0], p.uhi[0])) { tma_load_3d(ax, &mp.m[6], bar, zs, s.x0, o); ax += AUX; }
+                if (range_damped(o, 1, p.ulo[1], p.uhi[1])) { tma_load_3d(ax, &mp.m[7], bar, zs, s.x0, o); ax += AUX; }
+                if (range_damped(s.z0, 32, p.ulo[2], p.uhi[2])) tma_load_3d(ax, &mp.m[8], bar, zs, s.x0, o);
             });
         return;
     }
@@ -290,7 +294,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
       *pz = reinterpret_cast<S *>(p.pz);
     const uint32_t pstride = (uint32_t)p.ldz * (uint32_t)p.nnx;
     const T k[4] = {(T)C8_0, (T)C8_1, (T)C8_2, (T)C8_3};
-    const T dtx = (T)p.dtx, dty = (T)p.dty, dtz = (T)p.dtz;
+    const T dtx = scl<S>((T)p.dtx, p.spv), dty = scl<S>((T)p.dty, p.spv), dtz = scl<S>((T)p.dtz, p.spv);
     pipe_run<TX, L::KA, L::KB, 0>(
         p.sw, w0, w1, bars, ringB, p.err,
         [&](const Seg &s) {
@@ -372,7 +376,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             auto deriv = [&](int r, T2 &xx, T2 &zz) {
                 T2 zp[5];
 #pragma unroll
-                for (int m = 0; m < 5; ++m) zp[m] = ld2<T>(Bw, (xw + r) * 40 + zl + 2 * m);
+                for (int m = 0; m < 5; ++m)
+                    zp[m] = ld2<T>(Bw, (xw + r) * ZHalo<S>::W + (ZHalo<S>::ZH - MM) + zl + 2 * m);
                 const T zv[10] = {zp[0].a, zp[0].b, zp[1].a, zp[1].b, zp[2].a,
                                   zp[2].b, zp[3].a, zp[3].b, zp[4].a, zp[4].b};
                 T xa = 0, xb = 0, za = 0, zb = 0;
@@ -460,7 +465,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 }
                 if (yrec && (reca[r] | recb[r])) {  // ..iso..:294-304
                     const size_t tr = (size_t)trb[r] + (size_t)p.nx * (o - p.npml);
-                    T rr = reca[r] ? pa : pb;
+                    T rr = scl<S>(reca[r] ? pa : pb, p.rec_scale);
                     if (p.mute_nt && p.it < p.mute_nt[tr]) rr = T(0);
                     p.rec[tr * p.nt + p.it] = (float)rr;
                 }
@@ -491,8 +496,19 @@ static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
 }
 
 // configurations: (tile width, rows per warp) in {8, 16} x {1, 2} and (16, 4), two ring depths
+// 2-byte storage: tile shapes (8, 1), (16, 1), (16, 2) at ring depths 0 and 2
+template <class S>
+static cudaError_t launch_iso_half(const K1Launch &L, cudaStream_t st) {
+    if (L.depth == 1 || L.rows == 4 || (L.tx == 8 && L.rows != 1)) return cudaErrorInvalidConfiguration;
+    if (L.tx == 8) return L.depth ? launch_iso_t<8, S, 2, 1>(L, st) : launch_iso_t<8, S, 0, 1>(L, st);
+    if (L.rows == 1) return L.depth ? launch_iso_t<16, S, 2, 1>(L, st) : launch_iso_t<16, S, 0, 1>(L, st);
+    return L.depth ? launch_iso_t<16, S, 2, 2>(L, st) : launch_iso_t<16, S, 0, 2>(L, st);
+}
+
 cudaError_t launch_iso(const K1Launch &L, cudaStream_t st) {
     if (L.fp64) return launch_iso_t<8, double, 0, 2>(L, st);
+    if (L.half == 1) return launch_iso_half<__nv_bfloat16>(L, st);
+    if (L.half == 2) return launch_iso_half<__half>(L, st);
     // one of three ring depths for each (tile width, rows per lane) shape
 #define A3D_BY_DEPTH(TX_, R_)                                                   \
     return L.depth == 2 ? launch_iso_t<TX_, float, 2, R_>(L, st)                \

@@ -51,6 +51,13 @@ for _p in (PKG, os.path.join(ROOT, "oracle")):
 # written once + 2 parameters): 10 words = 40 B per cell update.
 KERNEL_BYTES = {"iso": (32.0, 28.0), "2o": (16.0, None), "vti": (40.0, 48.0), "tti": (56.0, 60.0)}
 STEP_BYTES = {"iso": 40.0, "2o": 16.0, "vti": 56.0, "tti": 60.0}
+# 2-byte wavefield storage (isotropic engine; the model parameters stay float):
+#   velocity sweep: P, u, v, w (2 B) + 1/rho (4 B) read, u, v, w written -> 18 B
+#   stress sweep:   u, v, w, P (2 B) + rho, vp (4 B) read, P written     -> 18 B
+#   unsplit step: (u, v, w, P) read and written at 2 B + 2 float parameters -> 24 B
+KERNEL_BYTES_2B = {"iso": (18.0, 18.0)}
+STEP_BYTES_2B = {"iso": 24.0}
+STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
 
 
 def smooth_model(n, seed, lo, hi, sigma=8.0):
@@ -230,10 +237,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error check")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--storage", default="fp32", choices=list(STORAGE),
+                    help="wavefield storage (bf16 / fp16: isotropic engine only; arithmetic stays fp32)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
     cfgd, models, shot, meta = workload(args.workload, args.nt or None)
+    meta["storage"] = args.storage
+    if args.storage != "fp32" and cfgd["physics"] != "iso":
+        raise SystemExit("2-byte storage is built for the isotropic engine only")
     if args.impl == "reference":
         run_reference(args, cfgd, models, shot, meta)
         return
@@ -253,7 +265,7 @@ def main():
     eng = cfgd["physics"]
     cfg = a3d.make_config(eng, cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"],
                           dz=cfgd["dz"], nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
-                          rec_z=cfgd.get("rec_z", -1), tile_x=args.tile_x)
+                          rec_z=cfgd.get("rec_z", -1), tile_x=args.tile_x, storage=STORAGE[args.storage])
     e = a3d.Engine(cfg, models, device=dev)
     # replicas: the job's shots run along x, one per rank, split round-robin as
     # the reference splits shots over nodes
@@ -290,18 +302,20 @@ def main():
 
     # ---- roofline of the dominant kernel
     peak, peak_kind = measured_peak()
-    kb = KERNEL_BYTES[eng]
+    two = args.storage != "fp32"
+    kb = (KERNEL_BYTES_2B if two else KERNEL_BYTES)[eng]
+    step_b = (STEP_BYTES_2B if two else STEP_BYTES)[eng]
     per = [kms[i] / kn[i] if kn[i] else 0.0 for i in range(2)]
     dom = 0 if (per[0] >= per[1] or kb[1] is None) else 1
     achieved = kb[dom] * cells / (per[dom] / 1000.0) / 1e9
-    step_gbs = STEP_BYTES[eng] * cells * nt * args.steps / (dev_ms / 1000.0) / 1e9
+    step_gbs = step_b * cells * nt * args.steps / (dev_ms / 1000.0) / 1e9
     kname = {("iso", 0): "iso_vel", ("iso", 1): "iso_stress", ("2o", 0): "k2o_step"}.get((eng, dom), "?")
-    tr = traffic_per_launch(meta["workload"])
+    tr = traffic_per_launch(meta["workload"] + ("" if args.storage == "fp32" else "_" + args.storage))
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": tr.get(kname) if isinstance(tr, dict) else None,
                 "peak_source": peak_kind, "bytes_per_cell": kb[dom],
                 "kernel_ms_per_launch": per[dom],
-                "step": {"bytes_per_cell": STEP_BYTES[eng], "achieved": step_gbs, "frac": step_gbs / peak}}
+                "step": {"bytes_per_cell": step_b, "achieved": step_gbs, "frac": step_gbs / peak}}
 
     # ---- FP64 error of the FP32 record (outside the timed region)
     rel = None
