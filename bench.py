@@ -68,6 +68,15 @@ def smooth_model(n, seed, lo, hi, sigma=8.0):
     return (lo + (hi - lo) * a).astype(np.float32)
 
 
+def smooth_field3(nx, ny, nz, seed, lo, hi, sigma=8.0):
+    """Gaussian-smoothed seeded noise mapped linearly to [lo, hi], shape (ny, nx, nz)."""
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    a = gaussian_filter(rng.standard_normal((ny, nx, nz)).astype(np.float32), sigma=sigma, mode="reflect")
+    a = (a - a.min()) / (a.max() - a.min())
+    return (lo + (hi - lo) * a).astype(np.float32)
+
+
 def workload(name, nt_override=None):
     if name == "iso256":
         n, dx, vmax = 256, 10.0, 4500.0
@@ -91,6 +100,40 @@ def workload(name, nt_override=None):
         return cfg, {"vel": vel}, (64, 64, 5), \
             dict(workload="2order_128cube_3layer_nt%d" % nt, model="128x128x128", dx_m=dx, nt=nt, dt_s=5e-4,
                  sponge=50, fm_hz=25.0, shot=[64, 64, 5], storage="fp32")
+    if name == "vti384":
+        # 384 x 384 x 256, d 12.5 m, nt 2500, 20-cell PML (the reference's compiled
+        # width), smooth seeded fields: v 1500-4500 (seed 3), Gardner density,
+        # epsilon 0-0.3 (seed 4), delta = min(delta', epsilon), delta' 0-0.15 (seed 5);
+        # dt = 0.4 d / (vmax sqrt(1.6)), 15 Hz Ricker at (24, 24, 2)
+        nx, ny, nz, d, vmax = 384, 384, 256, 12.5, 4500.0
+        vel = smooth_field3(nx, ny, nz, 3, 1500.0, vmax)
+        rho = (310.0 * vel.astype(np.float64) ** 0.25).astype(np.float32)
+        eps = smooth_field3(nx, ny, nz, 4, 0.0, 0.3)
+        dl = np.minimum(smooth_field3(nx, ny, nz, 5, 0.0, 0.15), eps).astype(np.float32)
+        dt = np.float32(0.4 * d / (vmax * np.sqrt(1.6)))
+        nt = nt_override or 2500
+        cfg = dict(physics="vti", nx=nx, ny=ny, nz=nz, dx=d, dy=d, dz=d, nt=nt, dt=float(dt), fm=15.0, npml=20)
+        return cfg, {"vel": vel, "rho": rho, "eps": eps, "del": dl}, (24, 24, 2), \
+            dict(workload="vti1order_384x384x256_nt%d" % nt, model="384x384x256", dx_m=d, nt=nt,
+                 dt_s=float(dt), npml=20, fm_hz=15.0, shot=[24, 24, 2], storage="fp32")
+    if name == "tti256":
+        # one 256^3 aperture of the TTI survey: d 12.5 m, nt 3000, 40-cell PML (the
+        # reference's compiled width), smooth seeded fields: v 1500-5000 (seed 7),
+        # epsilon 0-0.3 (seed 8), delta <= epsilon in 0-0.15 (seed 9), tilt 0-45 deg
+        # (seed 10), azimuth 0-360 deg (seed 11), in radians; 15 Hz Ricker at the
+        # aperture centre, z = 2
+        n, d, vmax = 256, 12.5, 5000.0
+        vel = smooth_field3(n, n, n, 7, 1500.0, vmax)
+        eps = smooth_field3(n, n, n, 8, 0.0, 0.3)
+        dl = np.minimum(smooth_field3(n, n, n, 9, 0.0, 0.15), eps).astype(np.float32)
+        th = smooth_field3(n, n, n, 10, 0.0, np.pi / 4)
+        ph = smooth_field3(n, n, n, 11, 0.0, 2 * np.pi)
+        dt = np.float32(0.4 * d / (vmax * np.sqrt(1.6)))
+        nt = nt_override or 3000
+        cfg = dict(physics="tti", nx=n, ny=n, nz=n, dx=d, dy=d, dz=d, nt=nt, dt=float(dt), fm=15.0, npml=40)
+        return cfg, {"vel": vel, "eps": eps, "del": dl, "theta": th, "phi": ph}, (n // 2, n // 2, 2), \
+            dict(workload="tti1order_256cube_nt%d" % nt, model="256x256x256", dx_m=d, nt=nt,
+                 dt_s=float(dt), npml=40, fm_hz=15.0, shot=[n // 2, n // 2, 2], storage="fp32")
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -231,7 +274,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="iso256", choices=["iso256", "2o128"])
+    ap.add_argument("--workload", default="iso256", choices=["iso256", "2o128", "vti384", "tti256"])
     ap.add_argument("--nt", type=int, default=0, help="override nt (profiling runs only)")
     ap.add_argument("--tile-x", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -309,7 +352,8 @@ def main():
     dom = 0 if (per[0] >= per[1] or kb[1] is None) else 1
     achieved = kb[dom] * cells / (per[dom] / 1000.0) / 1e9
     step_gbs = step_b * cells * nt * args.steps / (dev_ms / 1000.0) / 1e9
-    kname = {("iso", 0): "iso_vel", ("iso", 1): "iso_stress", ("2o", 0): "k2o_step"}.get((eng, dom), "?")
+    kname = {("iso", 0): "iso_vel", ("iso", 1): "iso_stress", ("2o", 0): "k2o_step", ("vti", 0): "vti_vel",
+             ("vti", 1): "vti_stress", ("tti", 0): "tti_vel", ("tti", 1): "tti_stress"}.get((eng, dom), "?")
     tr = traffic_per_launch(meta["workload"] + ("" if args.storage == "fp32" else "_" + args.storage))
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": tr.get(kname) if isinstance(tr, dict) else None,

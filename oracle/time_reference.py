@@ -21,7 +21,7 @@ sys.path.insert(0, ROOT)
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="iso256", choices=["iso256", "2o128"])
+    ap.add_argument("--workload", default="iso256", choices=["iso256", "2o128", "vti384", "tti256"])
     ap.add_argument("--steps", type=int, default=100)
     args = ap.parse_args()
     import bench
