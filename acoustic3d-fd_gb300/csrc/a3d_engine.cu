@@ -354,12 +354,15 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
             (rc = mk(&mvel[2], e->u, true, BOX_CORE)) || (rc = mk(&mvel[3], e->v, true, BOX_CORE)) ||
             (rc = mk(&mvel[4], e->w, true, BOX_CORE)) || (rc = mk(&mvel[5], e->rinv, false, BOX_CORE)))
             return rc;
-        e->nstr = 9;
+        e->nstr = 15;
         if ((rc = mk(&mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&mstr[1], e->u, true, BOX_HX)) ||
             (rc = mk(&mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&mstr[3], e->P, true, BOX_CORE)) ||
             (rc = mk(&mstr[4], e->Q, true, BOX_CORE)) || (rc = mk(&mstr[5], e->rho, false, BOX_CORE)) ||
             (rc = mk(&mstr[6], e->vp, false, BOX_CORE)) || (rc = mk(&mstr[7], e->eps, false, BOX_CORE)) ||
-            (rc = mk(&mstr[8], e->del, false, BOX_CORE)))
+            (rc = mk(&mstr[8], e->del, false, BOX_CORE)) || (rc = mk(&mstr[9], e->px, true, BOX_CORE)) ||
+            (rc = mk(&mstr[10], e->py, true, BOX_CORE)) || (rc = mk(&mstr[11], e->pz, true, BOX_CORE)) ||
+            (rc = mk(&mstr[12], e->qx, true, BOX_CORE)) || (rc = mk(&mstr[13], e->qy, true, BOX_CORE)) ||
+            (rc = mk(&mstr[14], e->qz, true, BOX_CORE)))
             return rc;
     } else {
         e->nvel = 9;
@@ -413,9 +416,9 @@ int a3d_engine::autotune() {
     const int fixed_tx = c.tile_x == 8 || c.tile_x == 16 ? c.tile_x : 0;
     // (tile width, rows per warp): the 2nd-order and isotropic kernels share tile
     // rows among a warp's lanes; the VTI/TTI kernels use one row per warp
-    const bool multirow = c.physics == A3D_2ORDER || c.physics == A3D_ISO;
+    const bool multirow = c.physics != A3D_TTI;  // TTI kernels: one row per warp
     std::vector<std::pair<int, int>> shapes;
-    if (multirow) shapes = {{8, 1}, {16, 1}, {8, 2}, {16, 2}, {16, 4}};
+    if (multirow) shapes = {{8, 1}, {16, 1}, {8, 2}, {16, 2}, {16, 4}};  // VTI skips (16, 4)
     else shapes = {{8, 1}, {16, 1}};
     // A3D_TUNE="tx,rows,depth,plan[;tx,rows,depth,plan]" pins the launch configuration of
     // each kernel kind (velocity; stress) instead of timing candidates
