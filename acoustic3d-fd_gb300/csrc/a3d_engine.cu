@@ -372,13 +372,16 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
             (rc = mk(&mvel[6], e->tst, false, BOX_CORE)) || (rc = mk(&mvel[7], e->tcp, false, BOX_CORE)) ||
             (rc = mk(&mvel[8], e->tsp, false, BOX_CORE)))
             return rc;
-        e->nstr = 12;
+        e->nstr = 18;
         if ((rc = mk(&mstr[0], e->u, true, BOX_H)) || (rc = mk(&mstr[1], e->v, true, BOX_H)) ||
             (rc = mk(&mstr[2], e->w, true, BOX_H)) || (rc = mk(&mstr[3], e->P, true, BOX_CORE)) ||
             (rc = mk(&mstr[4], e->Q, true, BOX_CORE)) || (rc = mk(&mstr[5], e->vp, false, BOX_CORE)) ||
             (rc = mk(&mstr[6], e->eps, false, BOX_CORE)) || (rc = mk(&mstr[7], e->del, false, BOX_CORE)) ||
             (rc = mk(&mstr[8], e->tct, false, BOX_CORE)) || (rc = mk(&mstr[9], e->tst, false, BOX_CORE)) ||
-            (rc = mk(&mstr[10], e->tcp, false, BOX_CORE)) || (rc = mk(&mstr[11], e->tsp, false, BOX_CORE)))
+            (rc = mk(&mstr[10], e->tcp, false, BOX_CORE)) || (rc = mk(&mstr[11], e->tsp, false, BOX_CORE)) ||
+            (rc = mk(&mstr[12], e->px, true, BOX_CORE)) || (rc = mk(&mstr[13], e->py, true, BOX_CORE)) ||
+            (rc = mk(&mstr[14], e->pz, true, BOX_CORE)) || (rc = mk(&mstr[15], e->qx, true, BOX_CORE)) ||
+            (rc = mk(&mstr[16], e->qy, true, BOX_CORE)) || (rc = mk(&mstr[17], e->qz, true, BOX_CORE)))
             return rc;
     }
     }
@@ -427,7 +430,7 @@ int a3d_engine::autotune() {
         for (int k = 0; k < 2; ++k) {
             int tx = 0, rows = 0, depth = 0, mode = 0, n = 0;
             if (sscanf(q, "%d,%d,%d,%d%n", &tx, &rows, &depth, &mode, &n) != 4 || (tx != 8 && tx != 16) ||
-                depth < 0 || depth > (multirow ? 2 : 1) ||
+                depth < 0 || depth > 2 ||
                 (rows != 1 && rows != 2 && rows != 4) || (rows == 4 && tx != 16) || mode < 0 || mode > 1)
                 return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[;...], got \"%s\"", env);
             if (!multirow && rows != 1) return fail(A3D_E_ARG, "A3D_TUNE: this physics runs one row per warp");
@@ -444,7 +447,7 @@ int a3d_engine::autotune() {
         for (int m = 0; m < 2; ++m) cand.push_back(Tune{8, 0, m, multirow ? 2 : 1});
     } else {
         for (auto sh : shapes)
-            for (int d = 0; d <= (multirow ? 2 : 1); ++d)
+            for (int d = 0; d <= 2; ++d)
                 for (int m = 0; m < 2; ++m)
                     if (!fixed_tx || sh.first == fixed_tx) cand.push_back(Tune{sh.first, d, m, sh.second});
     }

@@ -71,7 +71,7 @@ struct a3d_engine {
 
     // tensor maps for the two tile widths (index 0: 32x8 tiles, 1: 32x16)
     CUtensorMap m2o_cur[2][2], m2o_prev[2][2], m2o_vv[2];  // [tile][buffer]
-    CUtensorMap mvel[2][9], mstr[2][15];
+    CUtensorMap mvel[2][9], mstr[2][18];
     int nvel = 0, nstr = 0;
 
     // launch configuration per kernel kind ([0] velocity / 2nd-order step, [1] stress),

@@ -7,54 +7,7 @@ namespace a3d {
 
 template <int N> struct Maps { CUtensorMap m[N]; };
 
-template <class S>
-__device__ __forceinline__ size_t gidx(const K1Params &p, int iz, int ix, int iy) {
-    return (size_t)iz + (size_t)p.ldz * ((size_t)ix + (size_t)p.nnx * iy);
-}
-
-// the damped-axis pressure update shared by every 1st-order engine; the oracle's
-// engine form (a3d_oracle_loops.inc, engine_pupdate) performs the same operations
-template <class T, class S>
-__device__ __forceinline__ T pupdate(T Pold, T gx, T gy, T gz, bool dx, bool dy, bool dz,
-                                     float ax2, float ay2, float az2, S *cx, S *cy, S *cz,
-                                     size_t g) {
-    if (!(dx | dy | dz)) return ((Pold - gx) - gy) - gz;
-    T vx = dx ? from_store<T, S>(cx[g]) : T(0);
-    T vy = dy ? from_store<T, S>(cy[g]) : T(0);
-    T vz = dz ? from_store<T, S>(cz[g]) : T(0);
-    T s = Pold;
-    if (dx) s = s - vx;
-    if (dy) s = s - vy;
-    if (dz) s = s - vz;
-    if (!dx) s = s - gx;
-    if (!dy) s = s - gy;
-    if (!dz) s = s - gz;
-    if (dx) { vx = fma_t((T)ax2, vx, -gx); s = s + vx; cx[g] = to_store<S, T>(vx); }
-    if (dy) { vy = fma_t((T)ay2, vy, -gy); s = s + vy; cy[g] = to_store<S, T>(vy); }
-    if (dz) { vz = fma_t((T)az2, vz, -gz); s = s + vz; cz[g] = to_store<S, T>(vz); }
-    return s;
-}
-
 __device__ __forceinline__ bool damped(float a1, float a2) { return !(a1 == 1.0f && a2 == 1.0f); }
-
-// pupdate on split components already in registers (prefetched); the new
-// components come back in cx, cy, cz for the caller to store
-template <class T>
-__device__ __forceinline__ T pupdate_r(T Pold, T gx, T gy, T gz, bool dx, bool dy, bool dz, float ax2,
-                                       float ay2, float az2, T &cx, T &cy, T &cz) {
-    if (!(dx | dy | dz)) return ((Pold - gx) - gy) - gz;
-    T s = Pold;
-    if (dx) s = s - cx;
-    if (dy) s = s - cy;
-    if (dz) s = s - cz;
-    if (!dx) s = s - gx;
-    if (!dy) s = s - gy;
-    if (!dz) s = s - gz;
-    if (dx) { cx = fma_t((T)ax2, cx, -gx); s = s + cx; }
-    if (dy) { cy = fma_t((T)ay2, cy, -gy); s = s + cy; }
-    if (dz) { cz = fma_t((T)az2, cz, -gz); s = s + cz; }
-    return s;
-}
 
 // does the tile [a0, a0+len) of an axis touch its damped region?
 __device__ __forceinline__ bool range_damped(int a0, int len, int lo, int hi) {

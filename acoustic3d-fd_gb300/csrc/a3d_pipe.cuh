@@ -2,17 +2,12 @@
 //
 // A CTA owns a contiguous range of the sweep's (tile, plane) space (cta_range),
 // split into segments of consecutive output planes [ya, yb) of one 32 x TX tile.
-// For each segment it streams planes q = ya-4 .. yb+3 ("A items": the fields
-// whose y-derivative is taken, kept in a 9-plane register window) and, for
-// q >= ya+4, the output plane o = q-4 ("B items": everything else the update at
-// plane o reads).  One producer thread issues the TMA copies into two mbarrier
-// rings; the consumer warps (one 32-cell z row each) wait, compute, release.
-//
-//   A stage of item j is read at its own arrival (window push) and 4 items later
-//   (in-plane neighbours of output plane q-4), then released: KA >= 5.
-//   B stage is released right after the output plane is computed.
-//   Releases are per warp (the empty barriers count consumer warps): the warp
-//   converges, then its lane 0 arrives.
+// For each segment it streams planes q = ya-4 .. yb+3; item q carries the copy of
+// plane q of the fields whose y-derivative is taken ("A", kept in an 8-plane
+// register window) and, for q >= ya+4, everything else the update at the output
+// plane o = q-4 reads ("B").  One producer thread issues the TMA copies; the
+// consumer warps wait, compute, release (per warp: the warp converges, then its
+// lane 0 arrives on the empty barriers, which count consumer warps).
 //
 // Every wait is bounded (mbar_wait); a timeout records an error code, raises a
 // CTA-wide abort flag so the other role stops, and the producer drains all
@@ -23,26 +18,6 @@
 #include "a3d_common.cuh"
 
 namespace a3d {
-
-// ring depths: D = 0 — 8 A stages (4 live, 4 in flight) and 4 B stages;
-// D = 1 — 16 and 8, for more bytes in flight per CTA when fewer CTAs are resident
-template <int D> struct Depth {
-    static constexpr int KA = D ? 16 : 8;
-    static constexpr int KB = D ? 8 : 4;
-};
-
-template <int KA, int KB>
-struct PipeBars {
-    uint64_t fullA[KA], emptyA[KA], fullB[KB], emptyB[KB];
-    int abort_flag;
-    __device__ void init(int nconsumers) {  // nconsumers: consumer warps
-        for (int i = 0; i < KA; ++i) { mbar_init(&fullA[i], 1); mbar_init(&emptyA[i], nconsumers); }
-        for (int i = 0; i < KB; ++i) { mbar_init(&fullB[i], 1); mbar_init(&emptyB[i], nconsumers); }
-        abort_flag = 0;
-        fence_mbar_init();
-    }
-    __device__ volatile int *abort_ptr() { return &abort_flag; }
-};
 
 struct Seg {
     int tile, ya, yb, z0, x0;
@@ -63,87 +38,6 @@ __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long 
     s.z0 = MM + 32 * (s.tile % sw.ntz);
     s.x0 = MM + TX * (s.tile / sw.ntz);
     return s;
-}
-
-// Producer: one thread.  issueA(stage_ptr, bar, seg, q) / issueB(stage_ptr, bar, seg, o)
-// issue the copies of one item (the expect_tx byte counts are bytesA / bytesB; with
-// bytesB == 0 issueB posts its own expect_tx, for items whose size varies).
-template <int TX, int KA, int KB, class IssueA, class IssueB>
-__device__ __forceinline__ void pipe_produce(const Sweep &sw, long long w0, long long w1,
-                                             PipeBars<KA, KB> &b, unsigned char *ringA,
-                                             size_t strideA, uint32_t bytesA, unsigned char *ringB,
-                                             size_t strideB, uint32_t bytesB, int *err,
-                                             IssueA issueA, IssueB issueB) {
-    static_assert((KA & (KA - 1)) == 0 && (KB & (KB - 1)) == 0, "ring sizes are powers of two");
-    volatile int *ab = b.abort_ptr();
-    uint32_t ja = 0, jb = 0;
-    bool ok = true;
-    for (long long w = w0; w < w1 && ok;) {
-        long long wend;
-        const Seg s = make_seg<TX>(sw, w, w1, wend);
-        for (int q = s.ya - MM; q < s.yb + MM; ++q) {
-            const uint32_t sa = ja % KA;
-            if (ja >= KA)
-                ok = mbar_wait(&b.emptyA[sa], ((ja / KA) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab);
-            if (!ok) break;
-            mbar_arrive_expect_tx(&b.fullA[sa], bytesA);
-            issueA(ringA + sa * strideA, &b.fullA[sa], s, q);
-            ++ja;
-            const int o = q - MM;
-            if (o >= s.ya) {
-                const uint32_t sb = jb % KB;
-                if (jb >= KB)
-                    ok = mbar_wait(&b.emptyB[sb], ((jb / KB) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab);
-                if (!ok) break;
-                if (bytesB) mbar_arrive_expect_tx(&b.fullB[sb], bytesB);
-                issueB(ringB + sb * strideB, &b.fullB[sb], s, o);
-                ++jb;
-            }
-        }
-        w = wend;
-    }
-    // drain: every issued copy must land before the CTA's shared memory goes away
-    // (also after an abort: only the time limit ends these waits)
-    for (uint32_t j = (ja > KA ? ja - KA : 0); j < ja; ++j)
-        if (!mbar_wait(&b.fullA[j % KA], (j / KA) & 1, err, KERR_DRAIN_TIMEOUT, nullptr)) break;
-    for (uint32_t j = (jb > KB ? jb - KB : 0); j < jb; ++j)
-        if (!mbar_wait(&b.fullB[j % KB], (j / KB) & 1, err, KERR_DRAIN_TIMEOUT, nullptr)) break;
-}
-
-// Consumers: all consumer threads.  onSeg(seg) at a segment start; onLoad(stageA, seg, q)
-// when A item q arrived; onOut(stageA_of_o, stageB, seg, o) for each output plane.
-// Returns false on abort.
-template <int TX, int KA, int KB, class OnSeg, class OnLoad, class OnOut>
-__device__ __forceinline__ bool pipe_consume(const Sweep &sw, long long w0, long long w1,
-                                             PipeBars<KA, KB> &b, unsigned char *ringA,
-                                             size_t strideA, unsigned char *ringB, size_t strideB,
-                                             int *err, OnSeg onSeg, OnLoad onLoad, OnOut onOut) {
-    volatile int *ab = b.abort_ptr();
-    uint32_t ja = 0, jb = 0;
-    for (long long w = w0; w < w1;) {
-        long long wend;
-        const Seg s = make_seg<TX>(sw, w, w1, wend);
-        onSeg(s);
-        for (int q = s.ya - MM; q < s.yb + MM; ++q) {
-            const uint32_t sa = ja % KA;
-            if (!mbar_wait(&b.fullA[sa], (ja / KA) & 1, err, KERR_FULL_TIMEOUT, ab)) return false;
-            onLoad(ringA + sa * strideA, s, q);
-            const int o = q - MM;
-            if (o >= s.ya) {
-                const uint32_t sb = jb % KB;
-                if (!mbar_wait(&b.fullB[sb], (jb / KB) & 1, err, KERR_FULL_TIMEOUT, ab)) return false;
-                onOut(ringA + ((ja - MM) % KA) * strideA, ringB + sb * strideB, s, o);
-                __syncwarp();
-                if ((threadIdx.x & 31) == 0) mbar_arrive(&b.emptyB[sb]);
-                ++jb;
-            }
-            __syncwarp();
-            if (ja >= MM && (threadIdx.x & 31) == 0) mbar_arrive(&b.emptyA[(ja - MM) % KA]);
-            ++ja;
-        }
-        w = wend;
-    }
-    return true;
 }
 
 // ===========================================================================
