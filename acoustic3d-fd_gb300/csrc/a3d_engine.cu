@@ -733,7 +733,7 @@ static int validate(const a3d_config *c) {
     if (!(c->dx > 0) || !(c->dy > 0) || !(c->dz > 0) || !(c->dt > 0) || !(c->fm > 0))
         return fail(A3D_E_ARG, "dx, dy, dz, dt and fm must be positive");
     if (c->storage != A3D_FP32 && c->storage != A3D_FP64 &&
-        !((c->storage == A3D_BF16 || c->storage == A3D_FP16) && c->physics == A3D_ISO))
+        !((c->storage == A3D_BF16 || c->storage == A3D_FP16) && (c->physics == A3D_ISO || c->physics == A3D_VTI)))
         return fail(A3D_E_UNSUPPORTED, "storage type %d is not built for this engine", c->storage);
     if (c->physics == A3D_ISO && (c->wtype < 1 || c->wtype > 6))
         return fail(A3D_E_ARG, "wavelet type %d outside 1..6", c->wtype);

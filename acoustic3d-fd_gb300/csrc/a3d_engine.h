@@ -34,7 +34,7 @@ struct a3d_engine {
     int npml = 0;          // absorber cells (1st order) or sponge width npd (2nd order)
     int tx = 8;
     bool fp64 = false;
-    int half = 0;          // 2-byte wavefields: 1 bfloat16, 2 float16 (isotropic engine)
+    int half = 0;          // 2-byte wavefields: 1 bfloat16, 2 float16 (isotropic and VTI engines)
     size_t esz = 4;        // bytes per wavefield element
     // power-of-two storage scales of 2-byte wavefields: sig_v for u, v, w, sig_p for P
     // and its split components (1 otherwise)

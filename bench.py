@@ -51,12 +51,14 @@ for _p in (PKG, os.path.join(ROOT, "oracle")):
 # written once + 2 parameters): 10 words = 40 B per cell update.
 KERNEL_BYTES = {"iso": (32.0, 28.0), "2o": (16.0, None), "vti": (40.0, 48.0), "tti": (56.0, 60.0)}
 STEP_BYTES = {"iso": 40.0, "2o": 16.0, "vti": 56.0, "tti": 60.0}
-# 2-byte wavefield storage (isotropic engine; the model parameters stay float):
+# 2-byte wavefield storage (isotropic and VTI engines; the model parameters stay float):
 #   velocity sweep: P, u, v, w (2 B) + 1/rho (4 B) read, u, v, w written -> 18 B
 #   stress sweep:   u, v, w, P (2 B) + rho, vp (4 B) read, P written     -> 18 B
 #   unsplit step: (u, v, w, P) read and written at 2 B + 2 float parameters -> 24 B
-KERNEL_BYTES_2B = {"iso": (18.0, 18.0)}
-STEP_BYTES_2B = {"iso": 24.0}
+#   VTI: velocity P, Q, u, v, w (2 B) + 1/rho read, u, v, w written -> 20 B; stress
+#   u, v, w, P, Q (2 B) + rho, vp, eps, del read, P, Q written -> 30 B; step 36 B
+KERNEL_BYTES_2B = {"iso": (18.0, 18.0), "vti": (20.0, 30.0)}
+STEP_BYTES_2B = {"iso": 24.0, "vti": 36.0}
 STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
 
 
@@ -281,14 +283,14 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error check")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--storage", default="fp32", choices=list(STORAGE),
-                    help="wavefield storage (bf16 / fp16: isotropic engine only; arithmetic stays fp32)")
+                    help="wavefield storage (bf16 / fp16: isotropic and VTI engines; arithmetic stays fp32)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
     cfgd, models, shot, meta = workload(args.workload, args.nt or None)
     meta["storage"] = args.storage
-    if args.storage != "fp32" and cfgd["physics"] != "iso":
-        raise SystemExit("2-byte storage is built for the isotropic engine only")
+    if args.storage != "fp32" and cfgd["physics"] not in ("iso", "vti"):
+        raise SystemExit("2-byte storage is built for the isotropic and VTI engines only")
     if args.impl == "reference":
         run_reference(args, cfgd, models, shot, meta)
         return

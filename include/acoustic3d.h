@@ -101,7 +101,9 @@ typedef struct {
                           50 (2nd-order sponge), 20 (iso, VTI), 40 (TTI)          */
     int rec_z;         /* 2nd order: receiver depth in model cells; < 0: 1        */
     int mute;          /* zero the direct wave in the record                      */
-    int storage;       /* enum a3d_storage of the wavefields (FP32 or FP64 here)  */
+    int storage;       /* enum a3d_storage of the wavefields: FP32, FP64 (the FP64
+                          error-reference run), or BF16 / FP16 (isotropic and VTI:
+                          2-byte fields, float arithmetic)                        */
     int tile_x;        /* kernel tile width along x: 8 or 16 fixes it, 0 lets the
                           autotuner choose, < 0 disables the autotuner (32x8 tiles) */
 } a3d_config;

@@ -1,0 +1,66 @@
+"""Every launch configuration the autotuner can pick gives the same record.
+
+The autotuner chooses, per kernel kind and grid, a tile width, rows per lane, ring
+depth and sweep plan; the parity tests see only the configuration it picks on
+their grids.  Here each configuration is pinned (A3D_TUNE) in turn and its record
+compared bit for bit with the CPU oracle's engine form, on a grid with partial
+tiles in z and x, a y split into several chunks, and PML on every face.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import make_models
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = {  # (tile width, rows per lane) built per physics
+    "2o": [(8, 1), (16, 1), (8, 2), (16, 2), (16, 4)],
+    "iso": [(8, 1), (16, 1), (8, 2), (16, 2), (16, 4)],
+    "vti": [(8, 1), (16, 1), (8, 2), (16, 2)],
+    "tti": [(8, 1), (16, 1)],
+}
+CASE = {"2o": (30, 27, 45, (13, 11, 6), 70, 10), "iso": (30, 27, 45, (13, 11, 6), 70, 8),
+        "vti": (30, 27, 45, (13, 11, 6), 70, 8), "tti": (26, 23, 37, (11, 9, 5), 60, 8)}
+
+
+def _configs(eng):
+    out = []
+    for tx, rows in SHAPES[eng]:
+        for depth in (0, 1, 2):
+            for plan in (0, 1):
+                out.append(f"{tx},{rows},{depth},{plan}")
+    return out
+
+
+@pytest.fixture(autouse=True)
+def _clear_tune():
+    old = os.environ.pop("A3D_TUNE", None)
+    yield
+    os.environ.pop("A3D_TUNE", None)
+    if old is not None:
+        os.environ["A3D_TUNE"] = old
+
+
+@pytest.mark.parametrize("eng", ["2o", "iso", "vti", "tti"])
+def test_every_launch_configuration_matches_the_oracle(engine_lib, eng):
+    import a3d
+    nx, ny, nz, shot, nt, npml = CASE[eng]
+    models = make_models(eng, nx, ny, nz, seed=21)
+    s = O.Shot(nx, ny, nz, sx=shot[0], sy=shot[1], sz=shot[2], nt=nt, dt=1e-3, fm=25.0, npml=npml, rec_z=1,
+               mute=False, form=1)
+    ref, _ = O.run(eng, s, models, "f32")
+    cfg = a3d.make_config(eng, nx, ny, nz, nt=nt, dt=1e-3, fm=25.0, npml=npml, rec_z=1)
+    bad = []
+    for c in _configs(eng):
+        os.environ["A3D_TUNE"] = c if eng == "2o" else f"{c};{c}"
+        e = a3d.Engine(cfg, models)
+        try:
+            rec = e.run(*shot)
+        finally:
+            e.close()
+        if not np.array_equal(rec, ref):
+            bad.append((c, int(np.count_nonzero(rec != ref))))
+    assert not bad, f"configurations differing from the oracle: {bad}"
