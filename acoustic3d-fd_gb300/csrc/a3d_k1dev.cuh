@@ -19,6 +19,7 @@ __device__ __forceinline__ bool range_damped(int a0, int len, int lo, int hi) {
 template <class Kern, class... Args>
 static cudaError_t k1_launch(Kern kern, int nthreads, size_t smem, long long W, int grid,
                              cudaStream_t st, bool &attr_done, Args... args) {
+    if (!smem_fits(smem)) return cudaErrorInvalidConfiguration;
     if (!attr_done) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

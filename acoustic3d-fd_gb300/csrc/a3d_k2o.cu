@@ -223,6 +223,7 @@ static cudaError_t launch_k2o_t(const K2OLaunch &L, cudaStream_t st) {
     auto kern = k2o_step<TX, S, D, R>;
     constexpr int NT = 32 * (TX / (2 * R) + 1);
     static bool attr_done = false;
+    if (!smem_fits(SM::TOTAL)) return cudaErrorInvalidConfiguration;
     if (!attr_done) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)SM::TOTAL);

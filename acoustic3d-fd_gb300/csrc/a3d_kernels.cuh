@@ -72,4 +72,15 @@ size_t k2o_smem_bytes(int tx, bool fp64);
 // Fills sw.Yc and sw.W.
 int plan_sweep(Sweep &sw, int occ_per_sm, int mode);
 
+// does a CTA with this much dynamic shared memory fit on the current device?
+// (launchers return cudaErrorInvalidConfiguration for shapes that do not, which
+// the autotuner skips)
+inline bool smem_fits(size_t bytes) {
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return false;
+    return bytes <= (size_t)optin;
+}
+
 }  // namespace a3d

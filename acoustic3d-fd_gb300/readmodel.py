@@ -176,6 +176,7 @@ def _s(x):
 class FD:
     libname = None
     symbol = None
+    physics = None  # engine of the batched path: "2o", "iso", "vti", "tti"
 
     def __init__(self, model, sg, nt, dt, fpeak, snap_folder, snap_interval, wtype=1, device_i=0,
                  savesnap=False, nodei=0, cut_directwave=False):
@@ -264,8 +265,72 @@ class FD:
                 r.get()
 
 
+    # ---- batched path: one process per GPU feeding a3d_run_batch (replaces the
+    # process-per-shot pool and the nvidia-smi polling of readmodel.py:173-204)
+    _MODEL_FILES = {"vel": "vel_file", "rho": "rho_file", "eps": "epsilon_file", "del": "delta_file",
+                    "theta": "theta_file", "phi": "psi_file"}
+    _READS = {"2o": ("vel",), "iso": ("vel", "rho"), "vti": ("vel", "rho", "eps", "del"),
+              "tti": ("vel", "eps", "del", "theta", "phi")}
+
+    def engine_config(self):
+        """The engine configuration the legacy entry point of this class builds."""
+        import a3d
+        m = self.model
+        return a3d.make_config(self.physics, m.nx, m.ny, m.nz, dx=m.dx, dy=m.dy, dz=m.dz, nt=self.nt, dt=self.dt,
+                               fm=self.fpeak, wtype=self.wtype if self.physics == "iso" else 1, npml=0,
+                               rec_z=-1, mute=bool(self.cut_directwave) and self.physics != "2o")
+
+    def read_models(self):
+        m = self.model
+        n = m.nx * m.ny * m.nz
+        out = {}
+        for k in self._READS[self.physics]:
+            a = np.fromfile(getattr(m, self._MODEL_FILES[k]), dtype=np.float32, count=n)
+            if a.size != n:
+                raise A3DError(f"model file for {k} holds {a.size} of {n} floats")
+            out[k] = a
+        return out
+
+    def write_record(self, shotname, rec):
+        """The legacy writer's layout: iy (step dgy/dy), ix (step dgx/dx), it (step dgt/dt)."""
+        jx = int(self.sg.receiver_dx / self.model.dx)
+        jy = int(self.sg.receiver_dy / self.model.dy)
+        jt = int(np.float32(self.sg.receiver_dt) / np.float32(self.dt))
+        np.ascontiguousarray(rec[::jy, ::jx, ::jt], dtype=np.float32).tofile(shotname)
+
+    def _survey_worker(self, tasks, device, graph):
+        import a3d
+        if not tasks:
+            return 0
+        recs, _ = a3d.run_batch(self.engine_config(), self.read_models(), [tuple(t[:3]) for t in tasks],
+                                graph=graph, device=device)
+        for t, rec in zip(tasks, recs):
+            self.write_record(self.shot_name(t), rec)
+        return len(tasks)
+
+    def survey(self, devices=(0,), skip_existing=False, graph=True):
+        """Every shot of this node through the batched entry point: one worker process
+        per device, each with its round-robin share of the shots (as allocateNode splits
+        nodes, readmodel.py:121-126) in one a3d_run_batch call, records written in the
+        legacy layout.  With skip_existing, complete record files are kept (resume).
+        Snapshots are not taken on this path (run() takes them)."""
+        tasks = [t for t in self.sg.nodetask[self.nodei]
+                 if not (skip_existing and os.path.exists(self.shot_name(t)) and
+                         os.path.getsize(self.shot_name(t)) == self.record_bytes())]
+        devices = list(devices)
+        if len(devices) == 1:
+            return self._survey_worker(tasks, devices[0], graph)
+        from multiprocessing import get_context
+        ctx = get_context("spawn")
+        with ctx.Pool(len(devices)) as pool:
+            res = [pool.apply_async(self._survey_worker, (tasks[k::len(devices)], d, graph))
+                   for k, d in enumerate(devices)]
+            return sum(r.get() for r in res)
+
+
 class Acoustic3d1order(FD):
     libname, symbol = "acoustic1order.so", "cuda_3dfd_1order"
+    physics = "iso"
 
     def _args(self, ishot, shotname, device):
         m = self.model
@@ -279,6 +344,7 @@ class Acoustic3d1order(FD):
 
 class Acoustic3dvti(FD):
     libname, symbol = "acoustic1vti.so", "cuda_3dfd_vti"
+    physics = "vti"
 
     def _args(self, ishot, shotname, device):
         m = self.model
@@ -293,6 +359,7 @@ class Acoustic3dvti(FD):
 
 class Acoustic3d2order(FD):
     libname, symbol = "acoustic2order.so", "cuda_3dfd"
+    physics = "2o"
 
     def _args(self, ishot, shotname, device):
         m = self.model
@@ -308,6 +375,7 @@ class Acoustic3d2order(FD):
 
 class Acoustic3dtti(FD):
     libname, symbol = "acoustic1tti.so", "cuda_3dfd_tti"
+    physics = "tti"
 
     def _args(self, ishot, shotname, device):
         m = self.model

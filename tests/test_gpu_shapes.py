@@ -53,14 +53,20 @@ def test_every_launch_configuration_matches_the_oracle(engine_lib, eng):
                mute=False, form=1)
     ref, _ = O.run(eng, s, models, "f32")
     cfg = a3d.make_config(eng, nx, ny, nz, nt=nt, dt=1e-3, fm=25.0, npml=npml, rec_z=1)
-    bad = []
+    bad, ran, unfit = [], 0, []
     for c in _configs(eng):
         os.environ["A3D_TUNE"] = c if eng == "2o" else f"{c};{c}"
         e = a3d.Engine(cfg, models)
         try:
             rec = e.run(*shot)
+        except a3d.A3DError as err:  # rings larger than a CTA's shared memory
+            assert "invalid configuration" in str(err), str(err)
+            unfit.append(c)
+            continue
         finally:
             e.close()
+        ran += 1
         if not np.array_equal(rec, ref):
             bad.append((c, int(np.count_nonzero(rec != ref))))
     assert not bad, f"configurations differing from the oracle: {bad}"
+    assert ran >= len(unfit), f"too few configurations fit: {unfit}"
