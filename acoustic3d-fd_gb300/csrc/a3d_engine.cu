@@ -130,6 +130,13 @@ using namespace a3d;
 
 a3d_engine::~a3d_engine() {
     if (st) cudaStreamSynchronize(st);
+    if (snap_st) cudaStreamSynchronize(snap_st);
+    for (int k = 0; k < NSNAP; ++k) {
+        if (snap_ring_host[k]) cudaFreeHost(snap_ring_host[k]);
+        if (snap_cropped[k]) cudaEventDestroy(snap_cropped[k]);
+        if (snap_copied[k]) cudaEventDestroy(snap_copied[k]);
+    }
+    if (snap_st) cudaStreamDestroy(snap_st);
     for (cudaEvent_t ev : kev) cudaEventDestroy(ev);
     for (void *p : allocs) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
@@ -522,6 +529,22 @@ int a3d_engine::autotune() {
     return check_kernel_error(this);
 }
 
+// snapshot ring: slot 0 reuses the crop buffer allocated at setup; pinned host
+// buffers, the copy stream and the events are made at the first snapshot
+int a3d_engine::snap_setup() {
+    if (snap_st) return A3D_OK;
+    const size_t bytes = (size_t)cfg.nx * cfg.ny * cfg.nz * 4;
+    for (int k = 0; k < NSNAP; ++k) {
+        snap_ring_dev[k] = k == 0 ? snap_dev : (float *)dalloc(bytes);
+        if (!snap_ring_dev[k]) return fail(A3D_E_NOMEM, "snapshot buffer allocation failed");
+        CUDA_TRY(cudaMallocHost(&snap_ring_host[k], bytes));
+        CUDA_TRY(cudaEventCreateWithFlags(&snap_cropped[k], cudaEventDisableTiming));
+        CUDA_TRY(cudaEventCreateWithFlags(&snap_copied[k], cudaEventDisableTiming));
+    }
+    CUDA_TRY(cudaStreamCreateWithFlags(&snap_st, cudaStreamNonBlocking));
+    return A3D_OK;
+}
+
 int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, double *ms) {
     const a3d_config &c = cfg;
     if (s.sx < 0 || s.sx >= c.nx || s.sy < 0 || s.sy >= c.ny || s.sz < 0 || s.sz >= c.nz)
@@ -541,23 +564,52 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
                 mute[ix + (size_t)c.nx * iy] = mute_nt(ix, iy, s.sx, s.sy, s.sz, c.dx, c.dy, c.dz, c.dt, c.fm, v_mute);
         CUDA_TRY(cudaMemcpyAsync(d_mute, mute.data(), mute.size() * 4, cudaMemcpyHostToDevice, st));
     }
+    // snapshots: crop into ring slot k on the compute stream, copy to pinned host
+    // memory on the snapshot stream, hand over (in order) when slot k is needed
+    // again or after the loop; the compute stream waits only for the copy that
+    // last used the slot's device buffer
+    struct Pending { int slot, it; };
+    std::vector<Pending> queue;
+    size_t qhead = 0;
+    int nsnap = 0;
+    const size_t win = (size_t)c.nx * c.ny * c.nz;
+    auto hand_over = [&](size_t upto) -> int {  // deliver queue[qhead, upto)
+        for (; qhead < upto; ++qhead) {
+            const Pending &q = queue[qhead];
+            CUDA_TRY(cudaEventSynchronize(snap_copied[q.slot]));
+            if (hook->take) {
+                const int r = hook->take(q.it, snap_ring_host[q.slot]);
+                if (r) return r;
+            }
+        }
+        return A3D_OK;
+    };
     auto snapshot = [&](int it, const void *field) -> int {
         if (!hook || !hook->want || !hook->want(it)) return A3D_OK;
+        int r;
+        if ((r = snap_setup())) return r;
+        const int k = nsnap % NSNAP;
+        if (nsnap >= NSNAP && (r = hand_over(queue.size() - (NSNAP - 1)))) return r;  // slot k's last use
+        CUDA_TRY(cudaStreamWaitEvent(st, snap_copied[k], 0));
         const int pad = g.pad;
         const float sc = 1.0f / sig_p;  // exact: sig_p is a power of two
+        float *dst = snap_ring_dev[k];
         if (fp64)
-            crop_window<double><<<1024, 256, 0, st>>>((const double *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
+            crop_window<double><<<1024, 256, 0, st>>>((const double *)field, dst, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
         else if (half == 1)
-            crop_window<__nv_bfloat16><<<1024, 256, 0, st>>>((const __nv_bfloat16 *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
+            crop_window<__nv_bfloat16><<<1024, 256, 0, st>>>((const __nv_bfloat16 *)field, dst, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
         else if (half == 2)
-            crop_window<__half><<<1024, 256, 0, st>>>((const __half *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
+            crop_window<__half><<<1024, 256, 0, st>>>((const __half *)field, dst, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
         else
-            crop_window<float><<<1024, 256, 0, st>>>((const float *)field, snap_dev, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
+            crop_window<float><<<1024, 256, 0, st>>>((const float *)field, dst, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
         CUDA_TRY(cudaGetLastError());
-        snap_host.resize((size_t)c.nx * c.ny * c.nz);
-        CUDA_TRY(cudaMemcpyAsync(snap_host.data(), snap_dev, snap_host.size() * 4, cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
-        return hook->take ? hook->take(it, snap_host.data()) : A3D_OK;
+        CUDA_TRY(cudaEventRecord(snap_cropped[k], st));
+        CUDA_TRY(cudaStreamWaitEvent(snap_st, snap_cropped[k], 0));
+        CUDA_TRY(cudaMemcpyAsync(snap_ring_host[k], dst, win * 4, cudaMemcpyDeviceToHost, snap_st));
+        CUDA_TRY(cudaEventRecord(snap_copied[k], snap_st));
+        queue.push_back({k, it});
+        ++nsnap;
+        return A3D_OK;
     };
     // the time loop, bracketed by ev0/ev1; with graph mode (and no snapshot or
     // per-kernel events in the loop) it is captured into a CUDA graph first and the
@@ -703,6 +755,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         });
         if (rc) return rc;
     }
+    if (hook && (rc = hand_over(queue.size()))) return rc;
     if ((rc = check_kernel_error(this))) return rc;
     if (profiling) {
         const int per = c.physics == A3D_2ORDER ? 2 : 3;

@@ -66,8 +66,17 @@ struct a3d_engine {
 
     float *rec = nullptr;   // [ny][nx][nt]
     int *d_mute = nullptr;  // first unmuted sample per trace
-    float *snap_dev = nullptr;
-    std::vector<float> snap_host;
+    // snapshot pipeline: the model window is cropped on the device into one of
+    // NSNAP buffers, copied on a second stream into pinned host memory, and handed
+    // to the caller when a later snapshot needs the slot or the shot ends, so the
+    // time loop does not stop for it
+    static constexpr int NSNAP = 3;
+    float *snap_dev = nullptr;               // crop buffer of slot 0 (the others are allocated lazily)
+    float *snap_ring_dev[NSNAP] = {nullptr, nullptr, nullptr};
+    float *snap_ring_host[NSNAP] = {nullptr, nullptr, nullptr};  // pinned
+    cudaStream_t snap_st = nullptr;
+    cudaEvent_t snap_cropped[NSNAP] = {nullptr, nullptr, nullptr}, snap_copied[NSNAP] = {nullptr, nullptr, nullptr};
+    int snap_setup();
 
     // tensor maps for the two tile widths (index 0: 32x8 tiles, 1: 32x16)
     CUtensorMap m2o_cur[2][2], m2o_prev[2][2], m2o_vv[2];  // [tile][buffer]
