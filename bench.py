@@ -270,13 +270,76 @@ def run_reference(args, cfgd, models, shot, meta):
     print(json.dumps(line), flush=True)
 
 
+def tti_windows(nt_override=None):
+    """The TTI survey of uneven apertures: 512 x 512 x 320 model, d 12.5 m, nt 3000;
+    smooth seeded fields (v 1500-5000 seed 7, epsilon 0-0.3 seed 8, delta <= epsilon
+    in 0-0.15 seed 9, tilt 0-45 deg seed 10, azimuth 0-360 deg seed 11, radians);
+    48 windows with sizes uniform per axis in [160, 320] and placements uniform
+    inside the model (seed 12), each with its own 20-cell PML and a 15 Hz Ricker at
+    its centre, depth 2."""
+    nx, ny, nz, d, vmax = 512, 512, 320, 12.5, 5000.0
+    vel = smooth_field3(nx, ny, nz, 7, 1500.0, vmax)
+    eps = smooth_field3(nx, ny, nz, 8, 0.0, 0.3)
+    dl = np.minimum(smooth_field3(nx, ny, nz, 9, 0.0, 0.15), eps).astype(np.float32)
+    th = smooth_field3(nx, ny, nz, 10, 0.0, np.pi / 4)
+    ph = smooth_field3(nx, ny, nz, 11, 0.0, 2 * np.pi)
+    rng = np.random.default_rng(12)
+    wins, shots = [], []
+    for _ in range(48):
+        wx, wy, wz = (int(v) for v in rng.integers(160, 321, size=3))
+        x0 = int(rng.integers(0, nx - wx + 1))
+        y0 = int(rng.integers(0, ny - wy + 1))
+        z0 = int(rng.integers(0, nz - wz + 1))
+        wins.append((x0, y0, z0, wx, wy, wz))
+        shots.append((x0 + wx // 2, y0 + wy // 2, z0 + 2))
+    dt = np.float32(0.4 * d / (vmax * np.sqrt(1.6)))
+    nt = nt_override or 3000
+    cfg = dict(physics="tti", nx=nx, ny=ny, nz=nz, dx=d, dy=d, dz=d, nt=nt, dt=float(dt), fm=15.0, npml=20)
+    return cfg, {"vel": vel, "eps": eps, "del": dl, "theta": th, "phi": ph}, wins, shots
+
+
+def run_windows(args):
+    """Bench step = one a3d_run_batch call over --windows apertures (graph replay on)."""
+    import a3d
+    import build as pkg_build
+    pkg_build.build()
+    cfgd, models, wins, shots = tti_windows(args.nt or None)
+    k = max(1, min(args.windows, len(wins)))
+    cfg = a3d.make_config("tti", cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"], dz=cfgd["dz"],
+                          nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"])
+    nt = cfgd["nt"]
+    cells = sum((w[3] + 2 * 20 - 8) * (w[4] + 2 * 20 - 8) * (w[5] + 2 * 20 - 8) for w in wins[:k])
+    for _ in range(args.warmup):
+        a3d.run_batch(cfg, models, shots[:1], windows=wins[:1], graph=True)
+    dev_ms, wall = 0.0, 0.0
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            _, ms = a3d.run_batch(cfg, models, shots[:k], windows=wins[:k], graph=True)
+            wall += time.perf_counter() - t0
+            dev_ms += sum(ms)
+    value = cells * nt * args.steps / (dev_ms / 1000.0) / 1e9
+    line = {"metric": "Gpts/s", "value": value, "unit": "Gpts/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "tti1order_512x512x320_windows_nt%d" % nt, "windows": k,
+                       "window_sizes": [list(w[3:]) for w in wins[:k]], "npml": 20, "storage": "fp32",
+                       "graph": True},
+            "shots_per_hour": 3600.0 * k * args.steps / wall,
+            "e2e": {"value": cells * nt * args.steps / wall / 1e9, "unit": "Gpts/s",
+                    "call": "a3d_run_batch (host model, per-window crop, upload, loop, record download)"},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="iso256", choices=["iso256", "2o128", "vti384", "tti256"])
+    ap.add_argument("--workload", default="iso256", choices=["iso256", "2o128", "vti384", "tti256", "ttiwin"])
+    ap.add_argument("--windows", type=int, default=4, help="ttiwin: apertures per bench step (of 48)")
     ap.add_argument("--nt", type=int, default=0, help="override nt (profiling runs only)")
     ap.add_argument("--tile-x", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -287,6 +350,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
+    if args.workload == "ttiwin":
+        run_windows(args)
+        return
     cfgd, models, shot, meta = workload(args.workload, args.nt or None)
     meta["storage"] = args.storage
     if args.storage != "fp32" and cfgd["physics"] not in ("iso", "vti"):
