@@ -32,7 +32,14 @@ class Config(ctypes.Structure):
                 ("dx", ctypes.c_float), ("dy", ctypes.c_float), ("dz", ctypes.c_float),
                 ("nt", ctypes.c_int), ("dt", ctypes.c_float), ("fm", ctypes.c_float),
                 ("wtype", ctypes.c_int), ("npml", ctypes.c_int), ("rec_z", ctypes.c_int),
-                ("mute", ctypes.c_int), ("storage", ctypes.c_int), ("tile_x", ctypes.c_int)]
+                ("mute", ctypes.c_int), ("storage", ctypes.c_int), ("tile_x", ctypes.c_int),
+                ("boundary", ctypes.c_int)]
+
+
+BOUNDARY_PML, BOUNDARY_LEARNED = 0, 1
+BOUNDARIES = {"pml": BOUNDARY_PML, "learned": BOUNDARY_LEARNED}
+CLOSURE_NPARAM = 27792   # W1 [32][8][27], W2 [6][4][32][27], G [6][6][4]
+CLOSURE_PAD = 10         # rim-grid padding per face: 6 rim cells + 4 never updated
 
 
 class ShotPos(ctypes.Structure):
@@ -98,6 +105,38 @@ def lib() -> ctypes.CDLL:
         L.a3d_run_batch.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(ShotPos), ctypes.c_int,
                                     ctypes.POINTER(Opts)]
         L.a3d_run_batch.restype = ctypes.c_int
+        L.a3d_engine_set_closure.argtypes = [vp, _FP, ctypes.c_size_t]
+        L.a3d_engine_set_closure.restype = ctypes.c_int
+        L.a3d_engine_set_tap.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int, vp]
+        L.a3d_engine_set_tap.restype = ctypes.c_int
+        L.a3d_engine_closure_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]
+        L.a3d_engine_closure_times.restype = ctypes.c_int
+        L.a3d_closure_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.a3d_closure_create.restype = ctypes.c_int
+        L.a3d_closure_destroy.argtypes = [vp]
+        L.a3d_closure_destroy.restype = ctypes.c_int
+        L.a3d_closure_set_params.argtypes = [vp, _FP, ctypes.c_size_t]
+        L.a3d_closure_set_params.restype = ctypes.c_int
+        L.a3d_closure_get_params.argtypes = [vp, _FP, ctypes.c_size_t]
+        L.a3d_closure_get_params.restype = ctypes.c_int
+        L.a3d_closure_add_model.argtypes = [vp, _FP, _FP] + [ctypes.c_float] * 4 + [ctypes.POINTER(ctypes.c_int)]
+        L.a3d_closure_add_model.restype = ctypes.c_int
+        L.a3d_closure_add_sample.argtypes = [vp, ctypes.c_int, vp, vp]
+        L.a3d_closure_add_sample.restype = ctypes.c_int
+        L.a3d_closure_num_samples.argtypes = [vp]
+        L.a3d_closure_num_samples.restype = ctypes.c_int
+        L.a3d_closure_set_decay.argtypes = [vp, ctypes.c_float]
+        L.a3d_closure_set_decay.restype = ctypes.c_int
+        L.a3d_closure_staging.argtypes = [vp, ctypes.c_int]
+        L.a3d_closure_staging.restype = vp
+        L.a3d_closure_train.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_ulonglong, _FP]
+        L.a3d_closure_train.restype = ctypes.c_int
+        L.a3d_closure_eval.argtypes = [vp, ctypes.c_int, _FP, _FP, _FP]
+        L.a3d_closure_eval.restype = ctypes.c_int
+        L.a3d_closure_eval_tc.argtypes = [vp, ctypes.c_int, _FP]
+        L.a3d_closure_eval_tc.restype = ctypes.c_int
+        L.a3d_closure_teacher.argtypes = [vp, ctypes.c_int, _FP, _FP]
+        L.a3d_closure_teacher.restype = ctypes.c_int
         L.a3d_last_error.argtypes = []
         L.a3d_last_error.restype = ctypes.c_char_p
         _lib = L
@@ -120,10 +159,13 @@ def _fptr(a):
 
 
 def make_config(physics, nx, ny, nz, dx=10.0, dy=10.0, dz=10.0, nt=100, dt=1e-3, fm=20.0, wtype=1,
-                npml=0, rec_z=-1, mute=False, storage=FP32, tile_x=0) -> Config:
+                npml=0, rec_z=-1, mute=False, storage=FP32, tile_x=0, boundary=BOUNDARY_PML) -> Config:
     if isinstance(physics, str):
         physics = PHYSICS[physics]
-    return Config(physics, nx, ny, nz, dx, dy, dz, nt, dt, fm, wtype, npml, rec_z, int(mute), storage, tile_x)
+    if isinstance(boundary, str):
+        boundary = BOUNDARIES[boundary]
+    return Config(physics, nx, ny, nz, dx, dy, dz, nt, dt, fm, wtype, npml, rec_z, int(mute), storage, tile_x,
+                  boundary)
 
 
 class Engine:
@@ -200,6 +242,23 @@ class Engine:
         _check(lib().a3d_engine_describe(self.h, buf, len(buf)))
         return json.loads(buf.value.decode())
 
+    def set_closure(self, params):
+        """Install the learned rim's weights (engine created with boundary 'learned')."""
+        p = np.ascontiguousarray(params, dtype=np.float32).reshape(-1)
+        _check(lib().a3d_engine_set_closure(self.h, _fptr(p), p.size))
+
+    def set_tap(self, steps, off, dev_ptr):
+        """After each listed step copy u, v, w, P over [off, nn - off) to device memory."""
+        arr = (ctypes.c_int * max(len(steps), 1))(*steps)
+        _check(lib().a3d_engine_set_tap(self.h, arr, len(steps), off, ctypes.c_void_p(dev_ptr)))
+
+    def closure_times(self):
+        """(ms, launch pairs) of the closure summed since profiling was enabled."""
+        ms = ctypes.c_double(0.0)
+        n = ctypes.c_longlong(0)
+        _check(lib().a3d_engine_closure_times(self.h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
     def record_device_ptr(self) -> int:
         return lib().a3d_engine_record_device(self.h)
 
@@ -265,3 +324,90 @@ def run_batch(cfg: Config, models: dict, shots, windows=None, graph: bool = Fals
     out = [recs[offs[i]:offs[i] + dims[i][0] * dims[i][1] * cfg.nt].reshape(dims[i][0], dims[i][1], cfg.nt)
            for i in range(ns)]
     return out, [ms[i] for i in range(ns)]
+
+
+class Closure:
+    """Training object of the learned rim (a3d_closure_*): teacher state pairs of
+    nx*ny*nz models on the rim grid (model + 10 cells per face), trained on the GPU."""
+
+    def __init__(self, nx, ny, nz, device: int = 0):
+        self.shape = (ny + 2 * CLOSURE_PAD, nx + 2 * CLOSURE_PAD, nz + 2 * CLOSURE_PAD)  # (y, x, z)
+        h = ctypes.c_void_p()
+        _check(lib().a3d_closure_create(ctypes.byref(h), nx, ny, nz, device))
+        self.h = h
+        self.n = (nx, ny, nz)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().a3d_closure_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32).reshape(-1)
+        _check(lib().a3d_closure_set_params(self.h, _fptr(p), p.size))
+
+    def params(self):
+        p = np.zeros(CLOSURE_NPARAM, np.float32)
+        _check(lib().a3d_closure_get_params(self.h, _fptr(p), p.size))
+        return p
+
+    def add_model(self, vel, rho, dx, dy, dz, dt) -> int:
+        n = self.n[0] * self.n[1] * self.n[2]
+        v = np.ascontiguousarray(vel, np.float32).reshape(-1)
+        r = np.ascontiguousarray(rho, np.float32).reshape(-1)
+        if v.size != n or r.size != n:
+            raise ValueError("model arrays must hold nx*ny*nz values")
+        mid = ctypes.c_int(-1)
+        _check(lib().a3d_closure_add_model(self.h, _fptr(v), _fptr(r), dx, dy, dz, dt, ctypes.byref(mid)))
+        return mid.value
+
+    def staging(self, nstates) -> int:
+        """Device buffer of nstates rim-grid states (4 fields each), owned by the object."""
+        p = lib().a3d_closure_staging(self.h, nstates)
+        if not p:
+            raise A3DError(A3D_E_NOMEM, last_error())
+        return p
+
+    def state_floats(self) -> int:
+        return 4 * self.shape[0] * self.shape[1] * self.shape[2]
+
+    def add_sample(self, model, state0_ptr, state1_ptr):
+        _check(lib().a3d_closure_add_sample(self.h, model, ctypes.c_void_p(state0_ptr), ctypes.c_void_p(state1_ptr)))
+
+    def num_samples(self) -> int:
+        return lib().a3d_closure_num_samples(self.h)
+
+    def set_decay(self, decay):
+        _check(lib().a3d_closure_set_decay(self.h, decay))
+
+    def train(self, epochs, batch, lr, seed=0):
+        loss = np.zeros(epochs, np.float32)
+        _check(lib().a3d_closure_train(self.h, epochs, batch, lr, seed, _fptr(loss)))
+        return loss
+
+    def eval(self, sample):
+        """(correction [4, y, x, z], loss gradient [NPARAM], loss) of one sample."""
+        d = np.zeros((4,) + self.shape, np.float32)
+        g = np.zeros(CLOSURE_NPARAM, np.float32)
+        loss = np.zeros(1, np.float32)
+        _check(lib().a3d_closure_eval(self.h, sample, _fptr(d), _fptr(g), _fptr(loss)))
+        return d, g, float(loss[0])
+
+    def eval_tc(self, sample):
+        """The correction of one sample by the tensor-core kernels ([4, y, x, z])."""
+        d = np.zeros((4,) + self.shape, np.float32)
+        _check(lib().a3d_closure_eval_tc(self.h, sample, _fptr(d)))
+        return d
+
+    def teacher(self, sample):
+        """(step(S_t), S_t+1) of one sample, each [4, y, x, z]."""
+        x = np.zeros((4,) + self.shape, np.float32)
+        t = np.zeros((4,) + self.shape, np.float32)
+        _check(lib().a3d_closure_teacher(self.h, sample, _fptr(x), _fptr(t)))
+        return x, t

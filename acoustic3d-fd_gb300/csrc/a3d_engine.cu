@@ -269,7 +269,10 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     float *q = pm.data();
     const int n3[3] = {c.nx, c.ny, c.nz}, nn3[3] = {g.nnx, g.nny, g.nnz};
     for (int a = 0; a < 3; ++a) {
-        pml_profile(c.dt, d0, n3[a], e->npml, q, q + nn3[a], q + 2 * nn3[a], q + 3 * nn3[a]);
+        if (e->learned)  // undamped rim: every coefficient 1, the closure absorbs
+            std::fill(q, q + 4 * nn3[a], 1.0f);
+        else
+            pml_profile(c.dt, d0, n3[a], e->npml, q, q + nn3[a], q + 2 * nn3[a], q + 3 * nn3[a]);
         q += 4 * nn3[a];
     }
     {   // pressure-undamped interval of each axis (x, y, z)
@@ -734,7 +737,13 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         Ls.tx = tune[1].tx; Ls.depth = tune[1].depth; Ls.mode = tune[1].mode; Ls.rows = tune[1].rows;
         Lv.fp64 = Ls.fp64 = fp64; Lv.half = Ls.half = half; Lv.grid = Ls.grid = 0;
         auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
-        if ((rc = prepare_profiling(this, 3))) return rc;
+        if (learned && !cl_packed) return fail(A3D_E_ARG, "learned rim without a closure (a3d_engine_set_closure)");
+        std::vector<int> tap_slot(tap_out ? c.nt : 0, -1);
+        for (size_t k = 0; k < tap_slot.size() && k < tap_steps.size(); ++k)
+            if (tap_steps[k] >= 0 && tap_steps[k] < c.nt) tap_slot[tap_steps[k]] = (int)k;
+        const long long tbox = (long long)(g.nnz - 2 * tap_off) * (g.nnx - 2 * tap_off) * (g.nny - 2 * tap_off);
+        const int per = learned ? 4 : 3;
+        if ((rc = prepare_profiling(this, per))) return rc;
         rc = time_loop([&]() -> int {
             for (int it = 0; it < c.nt; ++it) {
                 p.it = it;
@@ -743,11 +752,24 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
                 p.amp1 = amp1[it] * sig_p;
                 Lv.p = p;
                 Ls.p = p;
-                if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it], st));
+                if (profiling) CUDA_TRY(cudaEventRecord(kev[per * it], st));
                 CUDA_TRY(launch(Lv, st));
-                if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 1], st));
+                if (profiling) CUDA_TRY(cudaEventRecord(kev[per * it + 1], st));
                 CUDA_TRY(launch(Ls, st));
-                if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 2], st));
+                if (profiling) CUDA_TRY(cudaEventRecord(kev[per * it + 2], st));
+                if (learned) {
+                    if (cl_simt)
+                        CUDA_TRY(cl_launch_apply(clg, (float *)u, (float *)v, (float *)w, (float *)P, cl_zinv, cl_kap,
+                                                 cl_packed, cl_h, st));
+                    else
+                        CUDA_TRY(cl_launch_apply_tc(clg, (float *)u, (float *)v, (float *)w, (float *)P, cl_zinv,
+                                                    cl_kap, cl_image, cl_packed + CL_NW1 + CL_NW2, cl_y, d_err, nullptr,
+                                                    0, g_sms, st));
+                    if (profiling) CUDA_TRY(cudaEventRecord(kev[per * it + 3], st));
+                }
+                if (!tap_slot.empty() && tap_slot[it] >= 0)
+                    CUDA_TRY(cl_launch_tap(g.nnz, g.nnx, g.nny, g.ldz, tap_off, (const float *)u, (const float *)v,
+                                           (const float *)w, (const float *)P, tap_out + 4 * tbox * tap_slot[it], st));
                 int r2 = snapshot(it, P);
                 if (r2) return r2;
             }
@@ -758,13 +780,18 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
     if (hook && (rc = hand_over(queue.size()))) return rc;
     if ((rc = check_kernel_error(this))) return rc;
     if (profiling) {
-        const int per = c.physics == A3D_2ORDER ? 2 : 3;
+        const int per = c.physics == A3D_2ORDER ? 2 : (learned ? 4 : 3);
         for (int it = 0; it < c.nt; ++it)
             for (int k = 0; k + 1 < per; ++k) {
                 float f = 0;
                 CUDA_TRY(cudaEventElapsedTime(&f, kev[per * it + k], kev[per * it + k + 1]));
-                kms[k] += f;
-                klaunch[k] += 1;
+                if (k < 2) {
+                    kms[k] += f;
+                    klaunch[k] += 1;
+                } else {
+                    cl_ms += f;
+                    cl_launch += 1;
+                }
             }
     }
     if (ms) {
@@ -790,6 +817,10 @@ static int validate(const a3d_config *c) {
         return fail(A3D_E_UNSUPPORTED, "storage type %d is not built for this engine", c->storage);
     if (c->physics == A3D_ISO && (c->wtype < 1 || c->wtype > 6))
         return fail(A3D_E_ARG, "wavelet type %d outside 1..6", c->wtype);
+    if (c->boundary != A3D_BOUNDARY_PML && c->boundary != A3D_BOUNDARY_LEARNED)
+        return fail(A3D_E_ARG, "unknown boundary %d", c->boundary);
+    if (c->boundary == A3D_BOUNDARY_LEARNED && (c->physics != A3D_ISO || c->storage != A3D_FP32))
+        return fail(A3D_E_UNSUPPORTED, "the learned rim is built for the isotropic engine with FP32 storage");
     return A3D_OK;
 }
 
@@ -824,8 +855,14 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
         if (e->cfg.rec_z >= cfg->nz) { delete e; return fail(A3D_E_ARG, "receiver depth %d outside the model", e->cfg.rec_z); }
         e->g.set(cfg->nx, cfg->ny, cfg->nz, MM + e->npml);
     } else {
-        e->npml = cfg->npml > 0 ? cfg->npml : (ph == A3D_TTI ? 40 : 20);
+        e->learned = cfg->boundary == A3D_BOUNDARY_LEARNED;
+        e->npml = cfg->npml > 0 ? cfg->npml : (e->learned ? CL_PAD : (ph == A3D_TTI ? 40 : 20));
         if (e->npml < 6) { delete e; return fail(A3D_E_ARG, "PML width %d below 6 cells", e->npml); }
+        if (e->learned && e->npml != CL_PAD) {
+            const int np = e->npml;
+            delete e;
+            return fail(A3D_E_ARG, "the learned rim pads by %d cells (npml %d given)", CL_PAD, np);
+        }
         e->g.set(cfg->nx, cfg->ny, cfg->nz, e->npml);
     }
     if (e->g.elems() > (size_t)INT32_MAX) {  // kernels index a field with 32-bit offsets
@@ -904,6 +941,79 @@ extern "C" int a3d_engine_set_profiling(a3d_engine *e, int on) {
     e->profiling = on != 0;
     e->kms[0] = e->kms[1] = 0;
     e->klaunch[0] = e->klaunch[1] = 0;
+    e->cl_ms = 0;
+    e->cl_launch = 0;
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_closure_times(const a3d_engine *e, double *ms, long long *launches) {
+    if (!e) return fail(A3D_E_ARG, "null engine");
+    if (ms) *ms = e->cl_ms;
+    if (launches) *launches = e->cl_launch;
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_set_closure(a3d_engine *e, const float *params, size_t n) {
+    clear_error();
+    if (!e || !params) return fail(A3D_E_ARG, "null engine or parameters");
+    if (!e->learned) return fail(A3D_E_ARG, "the engine was not created with boundary A3D_BOUNDARY_LEARNED");
+    if (n != (size_t)CL_NPARAM) return fail(A3D_E_ARG, "the closure takes %d parameters, got %zu", CL_NPARAM, n);
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(params[i])) return fail(A3D_E_ARG, "closure parameter %zu is not finite", i);
+    CUDA_TRY(cudaSetDevice(e->device));
+    if (!e->cl_packed) {
+        e->clg = cl_geom(e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz);
+        e->cl_packed = (float *)e->dalloc(CL_NPARAM * sizeof(float));
+        e->cl_zinv = (float *)e->dfield(4);
+        e->cl_kap = (float *)e->dfield(4);
+        const char *simt = getenv("A3D_CLOSURE_SIMT");
+        e->cl_simt = simt && simt[0] == '1';
+        if (e->cl_simt)
+            e->cl_h = (__nv_bfloat16 *)e->dalloc((size_t)e->clg.hoff[6] * CL_CH * sizeof(__nv_bfloat16));
+        else {
+            e->cl_image = (uint16_t *)e->dalloc(cl_tc_image_halves() * sizeof(uint16_t));
+            e->cl_y = (float4 *)e->dalloc((size_t)e->clg.hoff[6] * sizeof(float4));
+        }
+        if (!e->cl_packed || !e->cl_zinv || !e->cl_kap || (e->cl_simt ? !e->cl_h : (!e->cl_image || !e->cl_y))) {
+            e->cl_packed = nullptr;
+            return fail(A3D_E_NOMEM, "device allocation failed");
+        }
+        CUDA_TRY(cl_prepare());
+        CUDA_TRY(cl_tc_prepare());
+        const a3d_config &c = e->cfg;
+        const float courant = c.dt / std::min(c.dx, std::min(c.dy, c.dz));
+        CUDA_TRY(cl_launch_scales((const float *)e->field_alloc(e->rho, 4), (const float *)e->field_alloc(e->vp, 4),
+                                  courant,
+                                  (float *)e->field_alloc(e->cl_zinv, 4), (float *)e->field_alloc(e->cl_kap, 4),
+                                  e->g.elems(), e->st));
+    }
+    std::vector<float> pk(CL_NPARAM);
+    cl_pack_params(params, pk.data());
+    CUDA_TRY(cudaMemcpyAsync(e->cl_packed, pk.data(), CL_NPARAM * sizeof(float), cudaMemcpyHostToDevice, e->st));
+    if (e->cl_image) {
+        std::vector<uint16_t> img(cl_tc_image_halves());
+        cl_pack_tc(params, img.data());
+        CUDA_TRY(cudaMemcpyAsync(e->cl_image, img.data(), img.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, e->st));
+    }
+    CUDA_TRY(cudaStreamSynchronize(e->st));
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_set_tap(a3d_engine *e, const int *steps, int n, int off, float *dev_out) {
+    clear_error();
+    if (!e) return fail(A3D_E_ARG, "null engine");
+    if (n == 0) {
+        e->tap_steps.clear();
+        e->tap_out = nullptr;
+        return A3D_OK;
+    }
+    if (n < 0 || !steps || !dev_out) return fail(A3D_E_ARG, "taps need steps and an output buffer");
+    if (e->cfg.physics == A3D_2ORDER || e->esz != 4) return fail(A3D_E_UNSUPPORTED, "taps are built for 1st-order FP32 engines");
+    if (off < 0 || 2 * off >= std::min(e->g.nnz, std::min(e->g.nnx, e->g.nny)))
+        return fail(A3D_E_ARG, "tap offset %d leaves an empty box", off);
+    e->tap_steps.assign(steps, steps + n);
+    e->tap_off = off;
+    e->tap_out = dev_out;
     return A3D_OK;
 }
 

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../include/acoustic3d.h"
+#include "a3d_closure.h"
 #include "a3d_k1.cuh"
 #include "a3d_setup.h"
 
@@ -89,6 +90,25 @@ struct a3d_engine {
     Tune tune[2];
     bool tuned = false;
     int autotune();
+
+    // learned rim (boundary A3D_BOUNDARY_LEARNED): undamped 6-cell rim, corrected
+    // after every step by the closure (bfloat16-rounded weights in the kernels'
+    // layout, 1/(rho vp) and vp dt / min(d) on the padded grid, hidden activations)
+    bool learned = false;
+    a3d::ClGeom clg{};
+    float *cl_packed = nullptr, *cl_zinv = nullptr, *cl_kap = nullptr;
+    __nv_bfloat16 *cl_h = nullptr;   // CUDA-core path (A3D_CLOSURE_SIMT=1)
+    uint16_t *cl_image = nullptr;    // tensor-core path: per-face bfloat16 weight images
+    float4 *cl_y = nullptr;          // and per-face outputs
+    bool cl_simt = false;
+    double cl_ms = 0;
+    long long cl_launch = 0;
+
+    // teacher taps: after step tap_steps[k], u, v, w, P over [tap_off, nn - tap_off)
+    // go to tap_out + 4 k box cells
+    std::vector<int> tap_steps;
+    int tap_off = 0;
+    float *tap_out = nullptr;
 
     // replay each shot's time loop as one CUDA graph (ignored with snapshots or
     // per-kernel timing)

@@ -106,7 +106,13 @@ typedef struct {
                           2-byte fields, float arithmetic)                        */
     int tile_x;        /* kernel tile width along x: 8 or 16 fixes it, 0 lets the
                           autotuner choose, < 0 disables the autotuner (32x8 tiles) */
+    int boundary;      /* enum a3d_boundary: A3D_BOUNDARY_PML (0, the physics' own
+                          absorber) or A3D_BOUNDARY_LEARNED (isotropic, FP32: a 6-cell
+                          undamped rim corrected by the closure set with
+                          a3d_engine_set_closure; npml must be 10 or <= 0)          */
 } a3d_config;
+
+enum a3d_boundary { A3D_BOUNDARY_PML = 0, A3D_BOUNDARY_LEARNED = 1 };
 
 typedef struct {
     int sx, sy, sz;    /* shot position in model cells (sxbeg, sybeg, szbeg)      */
@@ -192,6 +198,77 @@ int a3d_engine_describe(a3d_engine *e, char *buf, size_t n);
 
 /* Message of the last failure on the calling thread ("" if none). */
 const char *a3d_last_error(void);
+
+/* ------------------------------------------------- learned absorbing rim */
+/* No counterpart in the reference, whose absorber is the split PML of
+ * ..iso..:263-291 (20 cells per face).  The learned rim pads the model by 10 cells
+ * per face: the outer 4 are never updated (as in every engine) and the inner 6 are
+ * updated without damping, then corrected after every step by a small network:
+ *
+ *   x      = [u, v, w, P/(rho vp), k u, k v, k w, k P/(rho vp)],  k = vp dt / min(d)
+ *   h_f    = relu(W1 * x)        3x3x3 conv, 8 -> 32 channels, no bias, on face f's box
+ *                                (depth -1..5 along its normal, zero outside)
+ *   y_f    = W2_f * h_f          3x3x3 conv, 32 -> 4 channels, one kernel per face
+ *   (u, v, w, P) += sum over the faces whose rim holds the cell of
+ *                   G_f[depth] . y_f  (channel 3 times rho vp)
+ *
+ * A3D_CLOSURE_NPARAM floats in this order: W1 [32][8][27], W2 [6][4][32][27],
+ * G [6][6][4]; a 3x3x3 tap index is ((dy+1)*3 + (dx+1))*3 + (dz+1); face
+ * f = 2*axis + side (axis 0 z, 1 x, 2 y; side 0 low, 1 high).  The kernels use
+ * the weights rounded to bfloat16, store h as bfloat16 and accumulate in float. */
+#define A3D_CLOSURE_NPARAM 27792
+
+/* Install the closure of an engine created with boundary = A3D_BOUNDARY_LEARNED
+ * (required before its first run). */
+int a3d_engine_set_closure(a3d_engine *e, const float *params, size_t n);
+
+/* Teacher taps: after each listed step (0-based, ascending or not) the engine
+ * copies u, v, w and P over the box [off, nn - off) of its padded grid, z fastest,
+ * into dev_out (device memory; step k of the list at dev_out + 4 * k * box cells).
+ * FP32 storage only.  n = 0 removes the taps. */
+int a3d_engine_set_tap(a3d_engine *e, const int *steps, int n, int off, float *dev_out);
+
+/* Device ms and launch pairs of the closure summed over runs with profiling on. */
+int a3d_engine_closure_times(const a3d_engine *e, double *ms, long long *launches);
+
+/* Training object: teacher state pairs on the rim grid of an nx*ny*nz model
+ * (model + 10 cells per face, dense, z fastest), the loss
+ *   sum over rim cells of |correction - (S_t+1 - step(S_t))|^2 / E,
+ * channel 3 divided by rho vp and E the rim energy of step(S_t) in the same units,
+ * where step is the engine's undamped update on the rim grid (zeros in its outer 4
+ * cells), and Adam on float master weights (bfloat16 rounding in every forward). */
+typedef struct a3d_closure a3d_closure;
+int a3d_closure_create(a3d_closure **out, int nx, int ny, int nz, int device);
+int a3d_closure_destroy(a3d_closure *c);
+int a3d_closure_set_params(a3d_closure *c, const float *params, size_t n);
+int a3d_closure_get_params(const a3d_closure *c, float *params, size_t n);
+/* a model (vel, rho: nx*ny*nz host arrays) and its time step; *model receives its id */
+int a3d_closure_add_model(a3d_closure *c, const float *vel, const float *rho, float dx, float dy, float dz,
+                          float dt, int *model);
+/* one teacher pair: device arrays of 4 rim-grid fields each (u, v, w, P), e.g. two
+ * consecutive taps of a wide-PML engine with off = its npml - 10, or a learned-rim
+ * engine's own state (off = 0) and the wide-PML state one step later.  A pair whose
+ * rim energy is not finite is refused (A3D_E_ARG). */
+int a3d_closure_add_sample(a3d_closure *c, int model, const float *state0_dev, const float *state1_dev);
+int a3d_closure_num_samples(const a3d_closure *c);
+/* device buffer owned by the object for nstates rim-grid states (4 fields each),
+ * e.g. the tap target of a wide-PML engine; NULL on failure.  A larger request
+ * replaces the buffer. */
+float *a3d_closure_staging(a3d_closure *c, int nstates);
+/* decoupled weight decay of W1 and W2 (w -= lr * decay * w every Adam step; 0 off) */
+int a3d_closure_set_decay(a3d_closure *c, float decay);
+/* epochs over the samples in seeded random order, minibatches of `batch` samples;
+ * loss_per_epoch (or NULL) receives the mean minibatch loss of each epoch */
+int a3d_closure_train(a3d_closure *c, int epochs, int batch, float lr, unsigned long long seed,
+                      float *loss_per_epoch);
+/* one sample: the correction of step(S_t) (4 rim-grid fields, zero off the rim),
+ * the gradient of its loss (A3D_CLOSURE_NPARAM) and the loss; any may be NULL */
+int a3d_closure_eval(a3d_closure *c, int sample, float *delta_host, float *grad_host, float *loss);
+/* the same correction computed by the engine's tensor-core kernels (tcgen05
+ * MMAs, bfloat16 operands, float accumulation) instead of the CUDA-core ones */
+int a3d_closure_eval_tc(a3d_closure *c, int sample, float *delta_host);
+/* step(S_t) and S_t+1 of one sample (4 rim-grid fields each; either may be NULL) */
+int a3d_closure_teacher(const a3d_closure *c, int sample, float *x_host, float *t_host);
 
 /* ------------------------------------------- 2nd-order step without allocation */
 
