@@ -98,49 +98,183 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<const uint32_t *>(&p);
 }
 
-// tile geometry of one face kind: z faces run (l0, l1, l2) = (a, t1, t2), x and y
-// faces (t1, a, t2); O = output block, H = O + 2 and X = O + 4 cells per axis
-struct Kind {
-    int O[3], H[3], X[3];
-    int p1, q1, m1;  // layer 1: first / last row position in the input tile, 128-row slices
-    int p2, q2, m2;  // layer 2: the same in the hidden tile
-};
-
-__device__ __forceinline__ Kind kind_of(int f) {
-    Kind k;
-    const bool zf = (f >> 1) == 0;
-    k.O[0] = zf ? 7 : B1;
-    k.O[1] = zf ? B1 : 7;
-    k.O[2] = B2;
-    for (int i = 0; i < 3; ++i) { k.H[i] = k.O[i] + 2; k.X[i] = k.O[i] + 4; }
-    k.p1 = 1 + k.X[0] * (1 + k.X[1]);
-    k.q1 = (k.X[0] - 2) + k.X[0] * ((k.X[1] - 2) + k.X[1] * (k.X[2] - 2));
-    k.m1 = (k.q1 - k.p1 + 128) / 128;
-    k.p2 = 1 + k.H[0] * (1 + k.H[1]);
-    k.q2 = (k.H[0] - 2) + k.H[0] * ((k.H[1] - 2) + k.H[1] * (k.H[2] - 2));
-    k.m2 = (k.q2 - k.p2 + 128) / 128;
-    return k;
-}
-
-// block-local cell l (output-block coordinates; halo cells lie outside [0, O)) ->
-// face coordinates (a = depth + 1, t1, t2)
-__device__ __forceinline__ void local_face(int f, int l0, int l1, int l2, int t10, int t20, int &a, int &t1,
-                                           int &t2) {
-    if ((f >> 1) == 0) {
-        a = l0;
-        t1 = t10 + l1;
-    } else {
-        t1 = t10 + l0;
-        a = l1;
+// compile-time tile geometry of face F: z faces run (l0, l1, l2) = (a, t1, t2),
+// x and y faces (t1, a, t2); O = output block, H = O + 2 and X = O + 4 cells per
+// axis; tap offsets are tile-linear constants, so descriptors step by immediates
+template <int F> struct Face {
+    static constexpr int A = F >> 1, SG = (F & 1) ? 1 : -1;
+    static constexpr int T1A = A == 0 ? 1 : 0, T2A = A == 2 ? 1 : 2;
+    static constexpr int O0 = A == 0 ? 7 : B1, O1 = A == 0 ? B1 : 7, O2 = B2;
+    static constexpr int H0 = O0 + 2, H1 = O1 + 2, H2 = O2 + 2;
+    static constexpr int X0 = O0 + 4, X1 = O1 + 4, X2 = O2 + 4;
+    static constexpr int P1 = 1 + X0 * (1 + X1);                               // first layer-1 row
+    static constexpr int Q1 = (X0 - 2) + X0 * ((X1 - 2) + X1 * (X2 - 2));      // last
+    static constexpr int M1 = (Q1 - P1 + 128) / 128;
+    static constexpr int P2 = 1 + H0 * (1 + H1);
+    static constexpr int Q2 = (H0 - 2) + H0 * ((H1 - 2) + H1 * (H2 - 2));
+    static constexpr int M2 = (Q2 - P2 + 128) / 128;
+    static_assert(X0 * X1 * X2 == XC && H0 * H1 * H2 == HC, "tile sizes");
+    // layer-1 step s: taps (l0 = -1, 0) or (+1, zero weights) at (l1, l2) row s / 2
+    static __host__ __device__ constexpr int off1(int s) {
+        return ((s & 1) ? 1 : -1) + X0 * (((s >> 1) % 3 - 1) + X1 * ((s >> 1) / 3 - 1));
     }
-    t2 = t20 + l2;
-}
+    // global tap t = ((dy+1)*3 + (dx+1))*3 + (dz+1) in block-local axes
+    static __host__ __device__ constexpr int d0(int t) { return A == 0 ? SG * (t % 3 - 1) : t % 3 - 1; }
+    static __host__ __device__ constexpr int d1(int t) {
+        return A == 0 ? (t / 3) % 3 - 1 : (A == 1 ? SG * ((t / 3) % 3 - 1) : SG * (t / 9 - 1));
+    }
+    static __host__ __device__ constexpr int d2(int t) { return A == 2 ? (t / 3) % 3 - 1 : t / 9 - 1; }
+    static __host__ __device__ constexpr int off2(int t) { return d0(t) + H0 * (d1(t) + H1 * d2(t)); }
+    // block-local cell -> face coordinates (a = depth + 1, t1, t2)
+    static __device__ __forceinline__ void face(int l0, int l1, int l2, int t10, int t20, int &a, int &t1,
+                                                int &t2) {
+        if (A == 0) { a = l0; t1 = t10 + l1; } else { t1 = t10 + l0; a = l1; }
+        t2 = t20 + l2;
+    }
+};
 
 struct Geo {
     ClGeom g;
     int toff[7];  // first tile of face f; toff[6] = tiles
     int nb1[6];   // blocks along t1 of face f
 };
+
+struct Ctx {
+    unsigned char *smem;
+    uint32_t s_x, s_h, s_w1, s_w2, tm;
+    uint64_t *bar;
+    volatile int *abort;
+    int *err;
+    int tid, warp, lane;
+};
+
+// one 7 x 16 x 8 block of face F: input tile, layer 1 into the hidden tile, layer 2
+// into y; returns false once the CTA has aborted
+template <int F>
+__device__ __noinline__ bool tile_pass(const ClGeom &g, int t10, int t20, const float *__restrict__ u,
+                                       const float *__restrict__ v, const float *__restrict__ w,
+                                       const float *__restrict__ P, const float *__restrict__ zinv,
+                                       const float *__restrict__ kap, float4 *__restrict__ y, const Ctx &cx,
+                                       uint32_t (&ph)[4]) {
+    using K = Face<F>;
+    const int T1 = g.T1[F], T2 = g.T2[F];
+    unsigned char *smem = cx.smem;
+    for (int i = cx.tid; i < XC; i += THREADS) {
+        const int m0 = i % K::X0, m1 = (i / K::X0) % K::X1, m2 = i / (K::X0 * K::X1);
+        int a, t1, t2;
+        K::face(m0 - 2, m1 - 2, m2 - 2, t10, t20, a, t1, t2);
+        int c[3];
+        c[K::A] = (F & 1) ? g.nn[K::A] - CL_PAD - 1 + a : CL_PAD - a;
+        c[K::T1A] = 4 + t1;
+        c[K::T2A] = 4 + t2;
+        uint4 q = make_uint4(0, 0, 0, 0);
+        if (c[K::T1A] < g.nn[K::T1A] && c[K::T2A] < g.nn[K::T2A]) {  // the other bounds hold by construction
+            float x[8];
+            load_x(u, v, w, P, zinv, kap, gidx(g, c[0], c[1], c[2]), x);
+            q = make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]),
+                           pack_bf16(x[6], x[7]));
+        }
+        *reinterpret_cast<uint4 *>(smem + OFF_X + i * 16) = q;
+    }
+    fence_proxy_async();
+    __syncthreads();
+
+    // ---- layer 1: h = relu(W1 * x) on the hidden tile
+    auto issue1 = [&](int m, int b) {
+        const uint64_t a0 = sdesc(cx.s_x + (K::P1 + 128 * m) * 16, 16, 128), b0 = sdesc(cx.s_w1, 512, 128);
+#pragma unroll
+        for (int s = 0; s < NK1; ++s)
+            mma(cx.tm + 32 * b, a0 + (uint64_t)(int64_t)K::off1(s), b0 + (uint64_t)(s * 64), idesc(128, 32), s > 0);
+        commit(&cx.bar[b]);
+    };
+    if (cx.tid == 0) {
+        fence_after();
+        issue1(0, 0);
+    }
+    for (int m = 0; m < K::M1; ++m) {
+        const int b = m & 1;
+        if (cx.tid == 0 && m + 1 < K::M1) {
+            fence_after();
+            issue1(m + 1, b ^ 1);
+        }
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&cx.bar[b], ph[b], cx.err, KERR_CLOSURE, cx.abort));
+        ph[b] ^= 1;
+        fence_after();
+        if (ok) {
+            const int qd = cx.warp & 3, hf = cx.warp >> 2;
+            float val[16];
+            ld16(cx.tm + 32 * b + 16 * hf + ((uint32_t)(32 * qd) << 16), val);
+            const int p = K::P1 + 128 * m + 32 * qd + cx.lane;
+            const int k0 = p % K::X0 - 1, k1 = (p / K::X0) % K::X1 - 1, k2 = p / (K::X0 * K::X1) - 1;
+            if (p <= K::Q1 && k0 >= 0 && k0 < K::H0 && k1 >= 0 && k1 < K::H1 && k2 >= 0 && k2 < K::H2) {
+                int a, t1, t2;
+                K::face(k0 - 1, k1 - 1, k2 - 1, t10, t20, a, t1, t2);
+                const bool in = a >= 0 && a < 7 && t1 >= 0 && t1 < T1 && t2 >= 0 && t2 < T2;
+                const int hk = k0 + K::H0 * (k1 + K::H1 * k2);
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const float *vv = val + 8 * c;
+                    uint4 q;
+                    q.x = in ? pack_bf16(fmaxf(vv[0], 0.0f), fmaxf(vv[1], 0.0f)) : 0u;
+                    q.y = in ? pack_bf16(fmaxf(vv[2], 0.0f), fmaxf(vv[3], 0.0f)) : 0u;
+                    q.z = in ? pack_bf16(fmaxf(vv[4], 0.0f), fmaxf(vv[5], 0.0f)) : 0u;
+                    q.w = in ? pack_bf16(fmaxf(vv[6], 0.0f), fmaxf(vv[7], 0.0f)) : 0u;
+                    *reinterpret_cast<uint4 *>(smem + OFF_H + ((2 * hf + c) * HS + hk) * 16) = q;
+                }
+            }
+        }
+        fence_before();
+        __syncthreads();
+        if (*cx.abort) return false;
+    }
+    fence_proxy_async();
+    __syncthreads();
+
+    // ---- layer 2: y_f = W2_f * h on the block's rim cells
+    auto issue2 = [&](int m, int b) {
+        const uint64_t a0 = sdesc(cx.s_h + (K::P2 + 128 * m) * 16, HS * 16, 128), b0 = sdesc(cx.s_w2, 256, 128);
+#pragma unroll
+        for (int t = 0; t < 27; ++t)
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+                mma(cx.tm + 64 + 16 * b, a0 + (uint64_t)(int64_t)(K::off2(t) + 2 * q * HS),
+                    b0 + (uint64_t)((t * 2 + q) * 32), idesc(128, 16), (t | q) != 0);
+        commit(&cx.bar[2 + b]);
+    };
+    if (cx.tid == 0) {
+        fence_after();
+        issue2(0, 0);
+    }
+    for (int m = 0; m < K::M2; ++m) {
+        const int b = m & 1;
+        if (cx.tid == 0 && m + 1 < K::M2) {
+            fence_after();
+            issue2(m + 1, b ^ 1);
+        }
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&cx.bar[2 + b], ph[2 + b], cx.err, KERR_CLOSURE, cx.abort));
+        ph[2 + b] ^= 1;
+        fence_after();
+        if (ok && cx.warp < 4) {
+            float val[16];
+            ld16(cx.tm + 64 + 16 * b + ((uint32_t)(32 * cx.warp) << 16), val);
+            const int p = K::P2 + 128 * m + 32 * cx.warp + cx.lane;
+            const int l0 = p % K::H0 - 1, l1 = (p / K::H0) % K::H1 - 1, l2 = p / (K::H0 * K::H1) - 1;
+            if (p <= K::Q2 && l0 >= 0 && l0 < K::O0 && l1 >= 0 && l1 < K::O1 && l2 >= 0 && l2 < K::O2) {
+                int a, t1, t2;
+                K::face(l0, l1, l2, t10, t20, a, t1, t2);
+                if (a >= 1 && a < 7 && t1 < T1 && t2 < T2) {
+                    const long long lin = K::A == 0 ? a + 7LL * (t1 + (long long)T1 * t2)
+                                                    : t1 + (long long)T1 * (a + 7LL * t2);
+                    y[g.hoff[F] + lin] = make_float4(val[0], val[1], val[2], val[3]);
+                }
+            }
+        }
+        fence_before();
+        __syncthreads();
+        if (*cx.abort) return false;
+    }
+    return true;
+}
 
 __global__ void __launch_bounds__(THREADS, 1)
     closure_tc(const __grid_constant__ Geo G, const float *__restrict__ u, const float *__restrict__ v,
@@ -151,10 +285,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + OFF_BAR);  // L1 x2, L2 x2, drain
     uint32_t *tmslot = reinterpret_cast<uint32_t *>(smem + OFF_BAR + 48);
     volatile int *abort = reinterpret_cast<volatile int *>(smem + OFF_BAR + 56);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const ClGeom &g = G.g;
     const uint32_t s_base = smem_u32(smem);
-    const uint32_t s_w1 = s_base + OFF_W1, s_w2 = s_base + OFF_W2, s_x = s_base + OFF_X, s_h = s_base + OFF_H;
 
     // zero the slack cells past the tiles once (rows of halo positions may read them)
     for (int i = tid; i < (XS - XC); i += THREADS)
@@ -176,152 +309,31 @@ __global__ void __launch_bounds__(THREADS, 1)
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tm = *tmslot;
+    const Ctx cx{smem, s_base + OFF_X, s_base + OFF_H, s_base + OFF_W1, s_base + OFF_W2, *tmslot, bar, abort, err,
+                 tid, warp, tid & 31};
     uint32_t ph[4] = {0, 0, 0, 0};
     int loaded = -1;  // face whose weight image is in shared memory
 
-    for (int tile = blockIdx.x; tile < G.toff[6] && !*abort; tile += gridDim.x) {
+    for (int tile = blockIdx.x; tile < G.toff[6]; tile += gridDim.x) {
         int f = 0;
         while (f < 5 && tile >= G.toff[f + 1]) ++f;
         const int bi = tile - G.toff[f];
         const int t10 = (bi % G.nb1[f]) * B1, t20 = (bi / G.nb1[f]) * B2;
-        const Kind K = kind_of(f);
-        const int T1 = g.T1[f], T2 = g.T2[f];
-        int A, t1a, t2a;
-        face_axes(f, A, t1a, t2a);
         if (f != loaded) {  // the face's weight image: layer-1 steps, then layer-2 taps
             const uint4 *src = image + (size_t)f * (IMAGE / 8);
             for (int i = tid; i < IMAGE / 8; i += THREADS) reinterpret_cast<uint4 *>(smem)[i] = src[i];
             loaded = f;
         }
-        // input tile: the eight bfloat16 channels of every cell of block + 2
-        for (int i = tid; i < XC; i += THREADS) {
-            const int m0 = i % K.X[0], m1 = (i / K.X[0]) % K.X[1], m2 = i / (K.X[0] * K.X[1]);
-            int a, t1, t2;
-            local_face(f, m0 - 2, m1 - 2, m2 - 2, t10, t20, a, t1, t2);
-            int c[3];
-            c[A] = (f & 1) ? g.nn[A] - CL_PAD - 1 + a : CL_PAD - a;
-            c[t1a] = 4 + t1;
-            c[t2a] = 4 + t2;
-            uint4 q = make_uint4(0, 0, 0, 0);
-            if (c[0] >= 0 && c[0] < g.nn[0] && c[1] >= 0 && c[1] < g.nn[1] && c[2] >= 0 && c[2] < g.nn[2]) {
-                float x[8];
-                load_x(u, v, w, P, zinv, kap, gidx(g, c[0], c[1], c[2]), x);
-                q = make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]),
-                               pack_bf16(x[6], x[7]));
-            }
-            *reinterpret_cast<uint4 *>(smem + OFF_X + i * 16) = q;
+        bool go;
+        switch (f) {
+            case 0: go = tile_pass<0>(g, t10, t20, u, v, w, P, zinv, kap, y, cx, ph); break;
+            case 1: go = tile_pass<1>(g, t10, t20, u, v, w, P, zinv, kap, y, cx, ph); break;
+            case 2: go = tile_pass<2>(g, t10, t20, u, v, w, P, zinv, kap, y, cx, ph); break;
+            case 3: go = tile_pass<3>(g, t10, t20, u, v, w, P, zinv, kap, y, cx, ph); break;
+            case 4: go = tile_pass<4>(g, t10, t20, u, v, w, P, zinv, kap, y, cx, ph); break;
+            default: go = tile_pass<5>(g, t10, t20, u, v, w, P, zinv, kap, y, cx, ph); break;
         }
-        fence_proxy_async();
-        __syncthreads();
-
-        // ---- layer 1: h = relu(W1 * x) on the hidden tile
-        auto issue1 = [&](int m, int b) {
-            const int p0 = K.p1 + 128 * m;
-            for (int s = 0; s < NK1; ++s) {
-                const int rho = s >> 1, dl1 = rho % 3 - 1, dl2 = rho / 3 - 1, dl0 = (s & 1) ? 1 : -1;
-                const int pos = p0 + dl0 + K.X[0] * (dl1 + K.X[1] * dl2);
-                mma(tm + 32 * b, sdesc(s_x + pos * 16, 16, 128), sdesc(s_w1 + s * 1024, 512, 128), idesc(128, 32),
-                    s > 0);
-            }
-            commit(&bar[b]);
-        };
-        if (tid == 0) {
-            fence_after();
-            issue1(0, 0);
-        }
-        for (int m = 0; m < K.m1; ++m) {
-            const int b = m & 1;
-            if (tid == 0 && m + 1 < K.m1 && !*abort) {
-                fence_after();
-                issue1(m + 1, b ^ 1);
-            }
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar[b], ph[b], err, KERR_CLOSURE, abort));
-            ph[b] ^= 1;
-            fence_after();
-            if (ok) {
-                const int qd = warp & 3, hf = warp >> 2;
-                float val[16];
-                ld16(tm + 32 * b + 16 * hf + ((uint32_t)(32 * qd) << 16), val);
-                const int p = K.p1 + 128 * m + 32 * qd + lane;
-                const int m0 = p % K.X[0], m1 = (p / K.X[0]) % K.X[1], m2 = p / (K.X[0] * K.X[1]);
-                const int k0 = m0 - 1, k1 = m1 - 1, k2 = m2 - 1;
-                if (p <= K.q1 && k0 >= 0 && k0 < K.H[0] && k1 >= 0 && k1 < K.H[1] && k2 >= 0 && k2 < K.H[2]) {
-                    int a, t1, t2;
-                    local_face(f, k0 - 1, k1 - 1, k2 - 1, t10, t20, a, t1, t2);
-                    const bool in = a >= 0 && a < 7 && t1 >= 0 && t1 < T1 && t2 >= 0 && t2 < T2;
-                    const int hk = k0 + K.H[0] * (k1 + K.H[1] * k2);
-#pragma unroll
-                    for (int c = 0; c < 2; ++c) {
-                        uint4 q;
-                        const float *vv = val + 8 * c;
-                        q.x = in ? pack_bf16(fmaxf(vv[0], 0.0f), fmaxf(vv[1], 0.0f)) : 0u;
-                        q.y = in ? pack_bf16(fmaxf(vv[2], 0.0f), fmaxf(vv[3], 0.0f)) : 0u;
-                        q.z = in ? pack_bf16(fmaxf(vv[4], 0.0f), fmaxf(vv[5], 0.0f)) : 0u;
-                        q.w = in ? pack_bf16(fmaxf(vv[6], 0.0f), fmaxf(vv[7], 0.0f)) : 0u;
-                        *reinterpret_cast<uint4 *>(smem + OFF_H + ((2 * hf + c) * HS + hk) * 16) = q;
-                    }
-                }
-            }
-            fence_before();
-            __syncthreads();
-            if (*abort) break;
-        }
-        fence_proxy_async();
-        __syncthreads();
-        if (*abort) break;
-
-        // ---- layer 2: y_f = W2_f * h on the block's rim cells
-        const int sg = (f & 1) ? 1 : -1;
-        auto issue2 = [&](int m, int b) {
-            const int p0 = K.p2 + 128 * m;
-            for (int t = 0; t < 27; ++t) {
-                const int dz = t % 3 - 1, dx = (t / 3) % 3 - 1, dy = t / 9 - 1;
-                int d0, d1, d2;
-                if (A == 0) { d0 = sg * dz; d1 = dx; d2 = dy; }
-                else if (A == 1) { d0 = dz; d1 = sg * dx; d2 = dy; }
-                else { d0 = dz; d1 = sg * dy; d2 = dx; }
-                const int pos = p0 + d0 + K.H[0] * (d1 + K.H[1] * d2);
-#pragma unroll
-                for (int q = 0; q < 2; ++q)
-                    mma(tm + 64 + 16 * b, sdesc(s_h + (2 * q * HS + pos) * 16, HS * 16, 128),
-                        sdesc(s_w2 + (t * 2 + q) * 512, 256, 128), idesc(128, 16), (t | q) != 0);
-            }
-            commit(&bar[2 + b]);
-        };
-        if (tid == 0) {
-            fence_after();
-            issue2(0, 0);
-        }
-        for (int m = 0; m < K.m2; ++m) {
-            const int b = m & 1;
-            if (tid == 0 && m + 1 < K.m2 && !*abort) {
-                fence_after();
-                issue2(m + 1, b ^ 1);
-            }
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar[2 + b], ph[2 + b], err, KERR_CLOSURE, abort));
-            ph[2 + b] ^= 1;
-            fence_after();
-            if (ok && warp < 4) {
-                float val[16];
-                ld16(tm + 64 + 16 * b + ((uint32_t)(32 * warp) << 16), val);
-                const int p = K.p2 + 128 * m + 32 * warp + lane;
-                const int k0 = p % K.H[0], k1 = (p / K.H[0]) % K.H[1], k2 = p / (K.H[0] * K.H[1]);
-                const int l0 = k0 - 1, l1 = k1 - 1, l2 = k2 - 1;
-                if (p <= K.q2 && l0 >= 0 && l0 < K.O[0] && l1 >= 0 && l1 < K.O[1] && l2 >= 0 && l2 < K.O[2]) {
-                    int a, t1, t2;
-                    local_face(f, l0, l1, l2, t10, t20, a, t1, t2);
-                    if (a >= 1 && a < 7 && t1 < T1 && t2 < T2) {
-                        const long long lin = A == 0 ? a + 7LL * (t1 + (long long)T1 * t2)
-                                                     : t1 + (long long)T1 * (a + 7LL * t2);
-                        y[g.hoff[f] + lin] = make_float4(val[0], val[1], val[2], val[3]);
-                    }
-                }
-            }
-            fence_before();
-            __syncthreads();
-            if (*abort) break;
-        }
+        if (!go) break;
     }
     // drain: every MMA this CTA issued has completed before its tensor memory is freed
     if (tid == 0) {
@@ -332,7 +344,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(TM_COLS));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(cx.tm), "r"(TM_COLS));
 }
 
 // rim cells: sum over the cell's faces of G_f[depth] . y_f, added to the fields

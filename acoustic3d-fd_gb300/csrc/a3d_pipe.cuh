@@ -19,11 +19,15 @@
 
 namespace a3d {
 
+// A segment's planes [ya, yb) are the pipeline's output planes; [oa, ob) are the
+// sweep's own output planes, the same range unless the pipeline runs EXT planes
+// beyond it on each side (the fused isotropic step computes velocities 4 planes
+// past the pressure planes it outputs).
 struct Seg {
-    int tile, ya, yb, z0, x0;
+    int tile, ya, yb, z0, x0, oa, ob;
 };
 
-template <int TX>
+template <int TX, int EXT = 0>
 __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long w1, long long &wend) {
     Seg s;
     const long long full = (long long)sw.ntz * sw.ntx * sw.Yc;  // units of a full chunk
@@ -37,6 +41,10 @@ __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long 
     s.yb = s.ya + (int)(wend - w);
     s.z0 = MM + 32 * (s.tile % sw.ntz);
     s.x0 = MM + TX * (s.tile / sw.ntz);
+    s.oa = s.ya;
+    s.ob = s.yb;
+    s.ya -= EXT;
+    s.yb += EXT;
     return s;
 }
 
@@ -108,7 +116,7 @@ struct Ring {
 // issue(sa, bdst, bbytes, bar, seg, q) posts the item's expect_tx on bar and
 // issues its copies: the A copy of plane q into A stage sa and, when bdst is not
 // null, the B copies of plane q-4 into bdst.
-template <int TX, int KA, int KB, size_t RB, class BSize, class Issue>
+template <int TX, int KA, int KB, size_t RB, int EXT = 0, class BSize, class Issue>
 __device__ __forceinline__ void pipe_produce_m(const Sweep &sw, long long w0, long long w1,
                                                PipeBarsM<KA, KB> &b, unsigned char *ringB, int *err,
                                                BSize bsize, Issue issue) {
@@ -118,7 +126,7 @@ __device__ __forceinline__ void pipe_produce_m(const Sweep &sw, long long w0, lo
     bool ok = true;
     for (long long w = w0; w < w1 && ok;) {
         long long wend;
-        const Seg s = make_seg<TX>(sw, w, w1, wend);
+        const Seg s = make_seg<TX, EXT>(sw, w, w1, wend);
         for (int q = s.ya - MM; q < s.yb + MM; ++q) {
             const uint32_t sa = ja % KA;
             if (ja >= KA && !(ok = mbar_wait(&b.emptyA[sa], ((ja / KA) - 1) & 1, err, KERR_EMPTY_TIMEOUT, ab)))
@@ -186,7 +194,7 @@ __device__ __forceinline__ void with_phase(int ph, F &&f) {
 //                                      (plane q-HOLD), the B item of output plane q-4 at bp;
 //                                      ph = item index mod 8 (run time: see with_phase)
 // Returns false on abort.
-template <int TX, int KA, int KB, int HOLD, class OnSeg, class Fill, class Step>
+template <int TX, int KA, int KB, int HOLD, int EXT = 0, class OnSeg, class Fill, class Step>
 __device__ __forceinline__ bool pipe_run(const Sweep &sw, long long w0, long long w1,
                                          PipeBarsM<KA, KB> &b, const unsigned char *ringB, int *err,
                                          OnSeg onSeg, Fill fill, Step step) {
@@ -197,7 +205,7 @@ __device__ __forceinline__ bool pipe_run(const Sweep &sw, long long w0, long lon
     bool ok = true;
     for (long long w = w0; w < w1;) {
         long long wend;
-        const Seg s = make_seg<TX>(sw, w, w1, wend);
+        const Seg s = make_seg<TX, EXT>(sw, w, w1, wend);
         onSeg(s);
         detail::static_for<0, 8>([&](auto ph) {
             if (!ok) return;

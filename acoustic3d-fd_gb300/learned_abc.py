@@ -257,7 +257,22 @@ def _main(argv=None):
     j.add_argument("--n", type=int, default=96)
     j.add_argument("--nt", type=int, default=1200)
     j.add_argument("--seed", type=int, default=1999)
+    r = sub.add_parser("run", help="one learned-rim shot on a seeded model (timing, profiling)")
+    r.add_argument("--params", default=PARAMS_FILE)
+    r.add_argument("--n", type=int, default=96)
+    r.add_argument("--nt", type=int, default=20)
+    r.add_argument("--seed", type=int, default=3)
     a = ap.parse_args(argv)
+    if a.cmd == "run":
+        md = S.iso_model(a.n, a.seed)
+        cfg = a3d.make_config("iso", a.n, a.n, a.n, 10.0, 10.0, 10.0, nt=a.nt, dt=S.cfl_dt(10.0, 4500.0), fm=20.0,
+                              npml=a3d.CLOSURE_PAD, boundary="learned", tile_x=16)
+        e = a3d.Engine(cfg, md)
+        e.set_closure(load_params(a.params))
+        _, ms = e.run(a.n // 2, a.n // 2, 8, with_time=True)
+        e.close()
+        print(json.dumps({"n": a.n, "nt": a.nt, "ms": ms}))
+        return
     if a.cmd == "train":
         mon = None
         if a.monitor_n:
