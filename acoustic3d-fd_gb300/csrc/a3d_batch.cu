@@ -54,7 +54,7 @@ extern "C" int a3d_run_batch(const a3d_problem *pb, const a3d_shot *shots, int n
     a3d_engine *e = nullptr;
     a3d_window cur{};
     a3d_engine::Tune tune[2];
-    bool have_tune = false;
+    bool have_tune = false, fused = false;
     size_t off = 0;
     int rc = A3D_OK;
     for (int i = 0; i < nshot && rc == A3D_OK; ++i) {
@@ -77,10 +77,12 @@ extern "C" int a3d_run_batch(const a3d_problem *pb, const a3d_shot *shots, int n
             }
             rc = a3d_engine_create(&e, &wc, wa[0], wa[1], wa[2], wa[3], wa[4], wa[5], o->device);
             if (rc) break;
-            if (have_tune) {  // launch shapes tuned on the first engine of the batch
+            if (have_tune) {  // launch shapes (and the isotropic step's form) tuned on the first engine
                 e->tune[0] = tune[0];
                 e->tune[1] = tune[1];
                 e->tuned = true;
+                if (fused && e->fused_ok) e->fused = true;
+                else if ((rc = e->drop_fused())) break;
             }
             cur = w;
         }
@@ -92,6 +94,7 @@ extern "C" int a3d_run_batch(const a3d_problem *pb, const a3d_shot *shots, int n
         if (!have_tune) {
             tune[0] = e->tune[0];
             tune[1] = e->tune[1];
+            fused = e->fused;
             have_tune = true;
         }
         if (o->rec_offsets) o->rec_offsets[i] = off;

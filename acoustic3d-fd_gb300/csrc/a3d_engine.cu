@@ -105,8 +105,8 @@ int make_field_map(CUtensorMap *m, const void *base, int dtype, const Grid &g, i
 
 // zhalo: width of z-halo'd boxes (40, or 48 for 2-byte storage: see ZHalo)
 static int box_dims(int box, int tx, int &b0, int &b1, int zhalo = 40) {
-    b0 = (box == BOX_HZ || box == BOX_H) ? zhalo : 32;
-    b1 = (box == BOX_HX || box == BOX_H) ? tx + 8 : tx;
+    b0 = box == BOX_H2 ? 48 : ((box == BOX_HZ || box == BOX_H) ? zhalo : 32);
+    b1 = box == BOX_H2 ? tx + 16 : ((box == BOX_HX || box == BOX_H) ? tx + 8 : tx);
     return 0;
 }
 
@@ -251,6 +251,8 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     if ((rc = field(&e->u)) || (rc = field(&e->v)) || (rc = field(&e->w)) || (rc = field(&e->P)) ||
         (rc = field(&e->px)) || (rc = field(&e->py)) || (rc = field(&e->pz)))
         return rc;
+    if (e->fused_ok && ((rc = field(&e->u2)) || (rc = field(&e->v2)) || (rc = field(&e->w2)) || (rc = field(&e->P2))))
+        return rc;
     if (c.physics != A3D_ISO) {
         if ((rc = field(&e->Q)) || (rc = field(&e->qx)) || (rc = field(&e->qy)) || (rc = field(&e->qz)))
             return rc;
@@ -358,6 +360,17 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
             (rc = mk(&mstr[6], e->px, true, BOX_CORE)) || (rc = mk(&mstr[7], e->py, true, BOX_CORE)) ||
             (rc = mk(&mstr[8], e->pz, true, BOX_CORE)))
             return rc;
+        for (int b = 0; b < 2 && e->fused_ok; ++b) {  // fused step reading set b
+            CUtensorMap *ms = e->mstep[t][b];
+            void *su = b ? e->u2 : e->u, *sv = b ? e->v2 : e->v, *sw = b ? e->w2 : e->w, *sp = b ? e->P2 : e->P;
+            if ((rc = mk(&ms[0], sp, true, BOX_H2)) || (rc = mk(&ms[1], su, true, BOX_HX)) ||
+                (rc = mk(&ms[2], sv, true, BOX_CORE)) || (rc = mk(&ms[3], sw, true, BOX_HZ)) ||
+                (rc = mk(&ms[4], e->rinv, false, BOX_H)) || (rc = mk(&ms[5], sp, true, BOX_CORE)) ||
+                (rc = mk(&ms[6], e->rho, false, BOX_CORE)) || (rc = mk(&ms[7], e->vp, false, BOX_CORE)) ||
+                (rc = mk(&ms[8], e->px, true, BOX_CORE)) || (rc = mk(&ms[9], e->py, true, BOX_CORE)) ||
+                (rc = mk(&ms[10], e->pz, true, BOX_CORE)))
+                return rc;
+        }
     } else if (c.physics == A3D_VTI) {
         e->nvel = 6;
         if ((rc = mk(&mvel[0], e->P, true, BOX_HX)) || (rc = mk(&mvel[1], e->Q, true, BOX_HZ)) ||
@@ -423,7 +436,51 @@ static int check_kernel_error(a3d_engine *e) {
 // timed launches each, CUDA events on the engine stream — and keeps the fastest.
 // Candidates that do not fit (shared memory) are skipped.  The wavefields hold
 // garbage afterwards; run() clears them before every shot.
+// The isotropic FP32 engine has two forms of its step: the two sweeps (velocity,
+// stress) and the fused sweep.  Unless A3D_FUSED or a pinned A3D_TUNE decides, both
+// are tuned and the faster one (summed launch times of the two sweeps against the
+// fused step's) runs.
 int a3d_engine::autotune() {
+    const char *fz = getenv("A3D_FUSED"), *pin = getenv("A3D_TUNE");
+    const bool forced = fz && (fz[0] == '0' || fz[0] == '1');
+    if (!fused_ok || forced || (pin && *pin && !fp64)) {
+        fused = fused_ok && fz && fz[0] == '1';
+        return autotune_form();
+    }
+    fused = false;
+    int rc = autotune_form();
+    if (rc) return rc;
+    const Tune two[2] = {tune[0], tune[1]};
+    fused = true;
+    if ((rc = autotune_form())) return rc;
+    if (tune[0].ms >= two[0].ms + two[1].ms) {
+        tune[0] = two[0];
+        tune[1] = two[1];
+        return drop_fused();
+    }
+    return A3D_OK;
+}
+
+// run the two-sweep form from now on; the second buffer set only serves the fused
+// step, so it is given back
+int a3d_engine::drop_fused() {
+    fused = false;
+    for (void **f : {&u2, &v2, &w2, &P2}) {
+        if (!*f) continue;
+        void *a = field_alloc(*f, esz);
+        auto it = std::find(allocs.begin(), allocs.end(), a);
+        if (it != allocs.end()) {
+            CUDA_TRY(cudaFree(a));
+            allocs.erase(it);
+            dev_bytes -= field_bytes(esz);
+        }
+        *f = nullptr;
+    }
+    fused_ok = false;
+    return A3D_OK;
+}
+
+int a3d_engine::autotune_form() {
     const a3d_config &c = cfg;
     std::vector<Tune> cand;
     const int fixed_tx = c.tile_x == 8 || c.tile_x == 16 ? c.tile_x : 0;
@@ -433,6 +490,8 @@ int a3d_engine::autotune() {
     std::vector<std::pair<int, int>> shapes;
     if (multirow) shapes = {{8, 1}, {16, 1}, {8, 2}, {16, 2}, {16, 4}};  // VTI skips (16, 4)
     else shapes = {{8, 1}, {16, 1}};
+    if (fused) shapes = {{8, 1}, {16, 1}, {8, 2}, {16, 2}};  // the fused step: ring depths 0 and 1
+    const int maxdepth = fused ? 1 : 2;
     // A3D_TUNE="tx,rows,depth,plan[;tx,rows,depth,plan]" pins the launch configuration of
     // each kernel kind (velocity; stress) instead of timing candidates
     if (const char *env = getenv("A3D_TUNE"); env && *env && !fp64) {
@@ -440,7 +499,7 @@ int a3d_engine::autotune() {
         for (int k = 0; k < 2; ++k) {
             int tx = 0, rows = 0, depth = 0, mode = 0, n = 0;
             if (sscanf(q, "%d,%d,%d,%d%n", &tx, &rows, &depth, &mode, &n) != 4 || (tx != 8 && tx != 16) ||
-                depth < 0 || depth > 2 ||
+                depth < 0 || depth > maxdepth || (fused && rows == 4) ||
                 (rows != 1 && rows != 2 && rows != 4) || (rows == 4 && tx != 16) || mode < 0 || mode > 1)
                 return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[;...], got \"%s\"", env);
             if (!multirow && rows != 1) return fail(A3D_E_ARG, "A3D_TUNE: this physics runs one row per warp");
@@ -457,11 +516,11 @@ int a3d_engine::autotune() {
         for (int m = 0; m < 2; ++m) cand.push_back(Tune{8, 0, m, multirow ? 2 : 1});
     } else {
         for (auto sh : shapes)
-            for (int d = 0; d <= 2; ++d)
+            for (int d = 0; d <= maxdepth; ++d)
                 for (int m = 0; m < 2; ++m)
                     if (!fixed_tx || sh.first == fixed_tx) cand.push_back(Tune{sh.first, d, m, sh.second});
     }
-    const int kinds = c.physics == A3D_2ORDER ? 1 : 2;
+    const int kinds = c.physics == A3D_2ORDER || fused ? 1 : 2;
     cudaEvent_t t0, t1;
     CUDA_TRY(cudaEventCreate(&t0));
     CUDA_TRY(cudaEventCreate(&t1));
@@ -506,6 +565,13 @@ int a3d_engine::autotune() {
                 L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
                 L.half = half;
                 p.svp = p.spv = p.rec_scale = 1.0f;
+                if (fused) {  // set 0 read, set 1 written
+                    L.kind = K1_ISO_STEP;
+                    L.maps = mstep[ti][0];
+                    L.nmaps = 11;
+                    L.out0 = u2; L.out1 = v2; L.out2 = w2; L.out3 = P2;
+                    return launch_iso_step(L, st);
+                }
                 auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
                 return launch(L, st);
             };
@@ -703,7 +769,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         });
         if (rc) return rc;
     } else {
-        void *fields[11] = {u, v, w, P, Q, px, py, pz, qx, qy, qz};
+        void *fields[15] = {u, v, w, P, Q, px, py, pz, qx, qy, qz, u2, v2, w2, P2};
         for (void *f : fields)
             if (f) CUDA_TRY(cudaMemsetAsync(field_alloc(f, esz), 0, fb, st));
         const int np = npml;
@@ -742,8 +808,38 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         for (size_t k = 0; k < tap_slot.size() && k < tap_steps.size(); ++k)
             if (tap_steps[k] >= 0 && tap_steps[k] < c.nt) tap_slot[tap_steps[k]] = (int)k;
         const long long tbox = (long long)(g.nnz - 2 * tap_off) * (g.nnx - 2 * tap_off) * (g.nny - 2 * tap_off);
-        const int per = learned ? 4 : 3;
+        const int per = fused ? 2 : (learned ? 4 : 3);
         if ((rc = prepare_profiling(this, per))) return rc;
+        if (fused) {  // one fused sweep per step; the buffer sets alternate
+            K1Launch Lf = Lv;
+            Lf.kind = K1_ISO_STEP;
+            Lf.nmaps = 11;
+            const int ti = tune[0].tx == 16 ? 1 : 0;
+            rc = time_loop([&]() -> int {
+                for (int it = 0; it < c.nt; ++it) {
+                    p.it = it;
+                    p.inj = inj[it];
+                    p.amp0 = amp0[it];
+                    p.amp1 = amp1[it];
+                    Lf.p = p;
+                    const int b = it & 1;
+                    Lf.maps = mstep[ti][b];
+                    void *nu = b ? u : u2, *nv = b ? v : v2, *nw = b ? w : w2, *np_ = b ? P : P2;
+                    Lf.out0 = nu; Lf.out1 = nv; Lf.out2 = nw; Lf.out3 = np_;
+                    if (profiling) CUDA_TRY(cudaEventRecord(kev[2 * it], st));
+                    CUDA_TRY(launch_iso_step(Lf, st));
+                    if (profiling) CUDA_TRY(cudaEventRecord(kev[2 * it + 1], st));
+                    if (!tap_slot.empty() && tap_slot[it] >= 0)
+                        CUDA_TRY(cl_launch_tap(g.nnz, g.nnx, g.nny, g.ldz, tap_off, (const float *)nu, (const float *)nv,
+                                               (const float *)nw, (const float *)np_, tap_out + 4 * tbox * tap_slot[it],
+                                               st));
+                    int r2 = snapshot(it, np_);
+                    if (r2) return r2;
+                }
+                return A3D_OK;
+            });
+            if (rc) return rc;
+        } else
         rc = time_loop([&]() -> int {
             for (int it = 0; it < c.nt; ++it) {
                 p.it = it;
@@ -780,7 +876,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
     if (hook && (rc = hand_over(queue.size()))) return rc;
     if ((rc = check_kernel_error(this))) return rc;
     if (profiling) {
-        const int per = c.physics == A3D_2ORDER ? 2 : (learned ? 4 : 3);
+        const int per = c.physics == A3D_2ORDER || fused ? 2 : (learned ? 4 : 3);
         for (int it = 0; it < c.nt; ++it)
             for (int k = 0; k + 1 < per; ++k) {
                 float f = 0;
@@ -858,6 +954,11 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
         e->learned = cfg->boundary == A3D_BOUNDARY_LEARNED;
         e->npml = cfg->npml > 0 ? cfg->npml : (e->learned ? CL_PAD : (ph == A3D_TTI ? 40 : 20));
         if (e->npml < 6) { delete e; return fail(A3D_E_ARG, "PML width %d below 6 cells", e->npml); }
+        {
+            const char *fz = getenv("A3D_FUSED");
+            e->fused_ok = ph == A3D_ISO && cfg->storage == A3D_FP32 && !e->learned && !(fz && fz[0] == '0');
+            e->fused = e->fused_ok && fz && fz[0] == '1';
+        }
         if (e->learned && e->npml != CL_PAD) {
             const int np = e->npml;
             delete e;
@@ -1034,10 +1135,10 @@ extern "C" int a3d_engine_describe(a3d_engine *e, char *buf, size_t n) {
         if (rc) return rc;
     }
     snprintf(buf, n,
-             "{\"grid\": [%d, %d, %d], \"ldz\": %d, \"pad\": %d, \"device_bytes\": %zu, "
+             "{\"grid\": [%d, %d, %d], \"ldz\": %d, \"pad\": %d, \"device_bytes\": %zu, \"fused\": %d, "
              "\"kernels\": [{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"ms\": %.4f}, "
              "{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"ms\": %.4f}]}",
-             e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, e->tune[0].tx, e->tune[0].rows,
+             e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, (int)e->fused, e->tune[0].tx, e->tune[0].rows,
              e->tune[0].depth, e->tune[0].mode, e->tune[0].ms, e->tune[1].tx, e->tune[1].rows,
              e->tune[1].depth, e->tune[1].mode, e->tune[1].ms);
     return A3D_OK;

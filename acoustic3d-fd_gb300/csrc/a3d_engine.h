@@ -54,6 +54,12 @@ struct a3d_engine {
     // wavefields
     void *X = nullptr, *Y = nullptr;                          // 2nd order
     void *u = nullptr, *v = nullptr, *w = nullptr, *P = nullptr, *Q = nullptr;
+    // fused isotropic step (FP32, PML): a second set of u, v, w, P; step it reads set
+    // it & 1 and writes the other (set 0 = u, v, w, P)
+    bool fused_ok = false;  // the fused step is built for this engine (buffers, maps)
+    bool fused = false;     // chosen: A3D_FUSED=1 forces it, =0 rules it out, else the autotuner decides
+    void *u2 = nullptr, *v2 = nullptr, *w2 = nullptr, *P2 = nullptr;
+    CUtensorMap mstep[2][2][11];  // [tile width][set read]
     void *px = nullptr, *py = nullptr, *pz = nullptr, *qx = nullptr, *qy = nullptr, *qz = nullptr;
 
     // coefficients
@@ -90,6 +96,8 @@ struct a3d_engine {
     Tune tune[2];
     bool tuned = false;
     int autotune();
+    int autotune_form();  // tunes the kernels of the current form (two sweeps, or the fused step)
+    int drop_fused();     // settle on the two-sweep form and free the fused step's buffers
 
     // learned rim (boundary A3D_BOUNDARY_LEARNED): undamped 6-cell rim, corrected
     // after every step by the closure (bfloat16-rounded weights in the kernels'

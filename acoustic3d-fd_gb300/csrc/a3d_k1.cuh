@@ -34,16 +34,17 @@ struct K1Params {
     float svp, spv, rec_scale;
 };
 
-enum K1Kind { K1_ISO_VEL = 0, K1_ISO_STR, K1_VTI_VEL, K1_VTI_STR, K1_TTI_VEL, K1_TTI_STR };
+enum K1Kind { K1_ISO_VEL = 0, K1_ISO_STR, K1_VTI_VEL, K1_VTI_STR, K1_TTI_VEL, K1_TTI_STR, K1_ISO_STEP };
 
-// tensor-map box shapes: core {32,TX}, x-halo {32,TX+8}, z-halo {40,TX}, both {40,TX+8}
-enum Box { BOX_CORE = 0, BOX_HX = 1, BOX_HZ = 2, BOX_H = 3 };
+// tensor-map box shapes: core {32,TX}, x-halo {32,TX+8}, z-halo {40,TX}, both {40,TX+8},
+// both doubled {48,TX+16} (the fused isotropic step's P tile)
+enum Box { BOX_CORE = 0, BOX_HX = 1, BOX_HZ = 2, BOX_H = 3, BOX_H2 = 4 };
 
 struct K1Launch {
     int kind;
     const CUtensorMap *maps;  // in the order the kernel documents
     int nmaps;
-    void *out0, *out1, *out2;  // fields written (vel: u,v,w; stress: P[,Q])
+    void *out0, *out1, *out2, *out3;  // fields written (vel: u,v,w; stress: P[,Q]; fused step: u,v,w,P)
     K1Params p;
     int tx, grid;
     bool fp64;
@@ -59,6 +60,7 @@ cudaError_t launch_k1(const K1Launch &L, cudaStream_t st);
 
 namespace a3d {
 cudaError_t launch_iso(const K1Launch &L, cudaStream_t st);
+cudaError_t launch_iso_step(const K1Launch &L, cudaStream_t st);  // fused isotropic step (FP32)
 cudaError_t launch_vti(const K1Launch &L, cudaStream_t st);
 cudaError_t launch_tti(const K1Launch &L, cudaStream_t st);
 }  // namespace a3d

@@ -58,6 +58,8 @@ STEP_BYTES = {"iso": 40.0, "2o": 16.0, "vti": 56.0, "tti": 60.0}
 #   VTI: velocity P, Q, u, v, w (2 B) + 1/rho read, u, v, w written -> 20 B; stress
 #   u, v, w, P, Q (2 B) + rho, vp, eps, del read, P, Q written -> 30 B; step 36 B
 KERNEL_BYTES_2B = {"iso": (18.0, 18.0), "vti": (20.0, 30.0)}
+#   fused isotropic step (FP32): u, v, w, P, 1/rho, rho, vp read, u, v, w, P written -> 44 B
+FUSED_BYTES = 44.0
 STEP_BYTES_2B = {"iso": 24.0, "vti": 36.0}
 STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
 
@@ -430,7 +432,8 @@ def main():
     barrier()
     kms, kn = e.kernel_times()
     e.set_profiling(False)
-    tuning = e.describe()["kernels"]
+    desc = e.describe()
+    tuning = desc["kernels"][:1] if desc.get("fused") else desc["kernels"]
     dev_ms = a3d_dist.max_over_ranks(dev_ms, group, f"cuda:{dev}" if group else None)
     cells = updated_cells(cfgd)
     nt = cfgd["nt"]
@@ -441,6 +444,8 @@ def main():
     peak, peak_kind = measured_peak()
     two = args.storage != "fp32"
     kb = (KERNEL_BYTES_2B if two else KERNEL_BYTES)[eng]
+    if desc.get("fused"):  # one fused step per time step: u, v, w, P, 1/rho, rho, vp read, u, v, w, P written
+        kb = (FUSED_BYTES, None)
     step_b = (STEP_BYTES_2B if two else STEP_BYTES)[eng]
     per = [kms[i] / kn[i] if kn[i] else 0.0 for i in range(2)]
     dom = 0 if (per[0] >= per[1] or kb[1] is None) else 1
@@ -448,6 +453,9 @@ def main():
     step_gbs = step_b * cells * nt * args.steps / (dev_ms / 1000.0) / 1e9
     kname = {("iso", 0): "iso_vel", ("iso", 1): "iso_stress", ("2o", 0): "k2o_step", ("vti", 0): "vti_vel",
              ("vti", 1): "vti_stress", ("tti", 0): "tti_vel", ("tti", 1): "tti_stress"}.get((eng, dom), "?")
+    if desc.get("fused"):
+        kname = "iso_step"
+    meta["fused_step"] = bool(desc.get("fused"))
     tr = traffic_per_launch(meta["workload"] + ("" if args.storage == "fp32" else "_" + args.storage))
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": tr.get(kname) if isinstance(tr, dict) else None,

@@ -18,18 +18,20 @@ pytestmark = pytest.mark.gpu
 
 SHAPES = {  # (tile width, rows per lane) built per physics
     "2o": [(8, 1), (16, 1), (8, 2), (16, 2), (16, 4)],
-    "iso": [(8, 1), (16, 1), (8, 2), (16, 2), (16, 4)],
+    "iso": [(8, 1), (16, 1), (8, 2), (16, 2), (16, 4)],          # the two-sweep step (A3D_FUSED=0)
+    "iso_fused": [(8, 1), (16, 1), (8, 2), (16, 2)],             # the fused step, ring depths 0 and 1
     "vti": [(8, 1), (16, 1), (8, 2), (16, 2)],
     "tti": [(8, 1), (16, 1)],
 }
 CASE = {"2o": (30, 27, 45, (13, 11, 6), 70, 10), "iso": (30, 27, 45, (13, 11, 6), 70, 8),
+        "iso_fused": (30, 27, 45, (13, 11, 6), 70, 8),
         "vti": (30, 27, 45, (13, 11, 6), 70, 8), "tti": (26, 23, 37, (11, 9, 5), 60, 8)}
 
 
 def _configs(eng):
     out = []
     for tx, rows in SHAPES[eng]:
-        for depth in (0, 1, 2):
+        for depth in ((0, 1) if eng == "iso_fused" else (0, 1, 2)):
             for plan in (0, 1):
                 out.append(f"{tx},{rows},{depth},{plan}")
     return out
@@ -38,24 +40,31 @@ def _configs(eng):
 @pytest.fixture(autouse=True)
 def _clear_tune():
     old = os.environ.pop("A3D_TUNE", None)
+    oldf = os.environ.pop("A3D_FUSED", None)
     yield
     os.environ.pop("A3D_TUNE", None)
+    os.environ.pop("A3D_FUSED", None)
     if old is not None:
         os.environ["A3D_TUNE"] = old
+    if oldf is not None:
+        os.environ["A3D_FUSED"] = oldf
 
 
-@pytest.mark.parametrize("eng", ["2o", "iso", "vti", "tti"])
+@pytest.mark.parametrize("eng", ["2o", "iso", "iso_fused", "vti", "tti"])
 def test_every_launch_configuration_matches_the_oracle(engine_lib, eng):
     import a3d
     nx, ny, nz, shot, nt, npml = CASE[eng]
-    models = make_models(eng, nx, ny, nz, seed=21)
+    phys = "iso" if eng == "iso_fused" else eng
+    if eng in ("iso", "iso_fused"):
+        os.environ["A3D_FUSED"] = "1" if eng == "iso_fused" else "0"
+    models = make_models(phys, nx, ny, nz, seed=21)
     s = O.Shot(nx, ny, nz, sx=shot[0], sy=shot[1], sz=shot[2], nt=nt, dt=1e-3, fm=25.0, npml=npml, rec_z=1,
                mute=False, form=1)
-    ref, _ = O.run(eng, s, models, "f32")
-    cfg = a3d.make_config(eng, nx, ny, nz, nt=nt, dt=1e-3, fm=25.0, npml=npml, rec_z=1)
+    ref, _ = O.run(phys, s, models, "f32")
+    cfg = a3d.make_config(phys, nx, ny, nz, nt=nt, dt=1e-3, fm=25.0, npml=npml, rec_z=1)
     bad, ran, unfit = [], 0, []
     for c in _configs(eng):
-        os.environ["A3D_TUNE"] = c if eng == "2o" else f"{c};{c}"
+        os.environ["A3D_TUNE"] = c if eng in ("2o", "iso_fused") else f"{c};{c}"
         e = a3d.Engine(cfg, models)
         try:
             rec = e.run(*shot)
