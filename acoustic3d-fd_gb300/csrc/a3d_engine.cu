@@ -328,16 +328,17 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     }
     // float16 storage scales (powers of two, so every rescaling is exact): P so that
     // the largest injected amplitude maps to 2^11 (headroom to the float16 maximum
-    // 65504); u, v, w by the velocity-to-pressure ratio dx rho / dt on top of that,
-    // so that both kinds of field sit in the same part of the float16 range.
-    // bfloat16 keeps float's exponent range and needs no scaling.
-    if (e->half == 2 && rho) {
+    // 65504); u, v, w by the velocity-to-pressure ratio dx rho / dt on top of that
+    // (rho = 1 for TTI, which has no density), so that both kinds of field sit in the
+    // same part of the float16 range.  bfloat16 keeps float's exponent range and
+    // needs no scaling.
+    if (e->half == 2) {
         float amax = 0.0f;
         for (int it = 0; it < c.nt; ++it)
             if (e->inj[it]) amax = std::max(amax, std::max(std::fabs(e->amp0[it]), std::fabs(e->amp1[it])));
         double rsum = 0.0;
         const size_t n = (size_t)c.nx * c.ny * c.nz;
-        for (size_t i = 0; i < n; ++i) rsum += rho[i];
+        for (size_t i = 0; i < n; ++i) rsum += rho ? rho[i] : 1.0f;
         const double rmean = rsum / (double)n;
         const double dmin = std::min(c.dx, std::min(c.dy, c.dz));
         if (amax > 0.0f) e->sig_p = std::ldexp(1.0f, (int)std::floor(std::log2(2048.0 / amax)));
@@ -915,7 +916,7 @@ static int validate(const a3d_config *c) {
     if (!(c->dx > 0) || !(c->dy > 0) || !(c->dz > 0) || !(c->dt > 0) || !(c->fm > 0))
         return fail(A3D_E_ARG, "dx, dy, dz, dt and fm must be positive");
     if (c->storage != A3D_FP32 && c->storage != A3D_FP64 &&
-        !((c->storage == A3D_BF16 || c->storage == A3D_FP16) && (c->physics == A3D_ISO || c->physics == A3D_VTI)))
+        !((c->storage == A3D_BF16 || c->storage == A3D_FP16) && c->physics != A3D_2ORDER))
         return fail(A3D_E_UNSUPPORTED, "storage type %d is not built for this engine", c->storage);
     if (c->physics == A3D_ISO && (c->wtype < 1 || c->wtype > 6))
         return fail(A3D_E_ARG, "wavelet type %d outside 1..6", c->wtype);

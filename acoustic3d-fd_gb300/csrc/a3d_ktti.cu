@@ -6,6 +6,8 @@
 //   tti_stress: the same rotation of D-u, D-v, D-w, then the VTI coefficients
 //               without density (..tti..:115-201), record + mute fused.
 // cos/sin of theta and phi are evaluated once at setup (float), not per step.
+// Wavefields may be stored in 2 bytes (bfloat16, or float16 with power-of-two
+// scales folded into the coefficients); the arithmetic stays float.
 #include <climits>
 
 #include "a3d_k1dev.cuh"
@@ -16,7 +18,7 @@ namespace a3d {
 // tti_vel: maps {P (H), Q (H), u, v, w (core), ct, st, cp, sp (core float)}
 template <int TX, class S, int D>
 struct TtiVelL {
-    static constexpr int AW = 40, AH = TX + 8;
+    static constexpr int AW = ZHalo<S>::W, AH = TX + 8;  // P / Q tile [AH][AW], z halo ZH
     static constexpr uint32_t C = 32 * TX, H = AW * AH;
     static constexpr uint32_t A_BYTES = 2 * H * sizeof(S);  // P tile, then Q tile
     static constexpr uint32_t B_BYTES = 3 * C * sizeof(S) + 4 * C * 4;
@@ -69,6 +71,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     using T = typename Arith<S>::T;
     using T2 = Two<T>;
     constexpr int NW = TX / (2 * R), NC = 32 * NW, AW = L::AW;
+    constexpr int ZS = WFieldZShift<S>::v;  // z offset of wavefield maps (2-byte storage)
+    constexpr int ZH = ZHalo<S>::ZH;        // first z cell of the tile inside a P / Q row
     static_assert(NW >= 1, "a warp covers 2R tile rows");
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<typename L::Bars *>(smem + L::BAR_OFF);
@@ -89,18 +93,19 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             [&](uint32_t sa, unsigned char *dst, uint32_t, uint64_t *bar, const Seg &s, int q) {
                 mbar_arrive_expect_tx(bar, L::A_BYTES + (dst ? L::B_BYTES : 0u));
                 unsigned char *a = ringA + sa * L::A_STRIDE;
-                tma_load_3d(a, &mp.m[0], bar, s.z0 - MM, s.x0 - MM, q);
-                tma_load_3d(a + L::H * sizeof(S), &mp.m[1], bar, s.z0 - MM, s.x0 - MM, q);
+                tma_load_3d(a, &mp.m[0], bar, s.z0 - ZH + ZS, s.x0 - MM, q);
+                tma_load_3d(a + L::H * sizeof(S), &mp.m[1], bar, s.z0 - ZH + ZS, s.x0 - MM, q);
                 if (!dst) return;
                 const int o = q - MM;
-                for (int k = 0; k < 3; ++k) tma_load_3d(dst + k * L::C * sizeof(S), &mp.m[2 + k], bar, s.z0, s.x0, o);
+                for (int k = 0; k < 3; ++k)
+                    tma_load_3d(dst + k * L::C * sizeof(S), &mp.m[2 + k], bar, s.z0 + ZS, s.x0, o);
                 for (int k = 0; k < 4; ++k) tma_load_3d(dst + oF + k * L::C * 4, &mp.m[5 + k], bar, s.z0, s.x0, o);
             });
         return;
     }
 
     const int zl = 2 * (lane & 15), xw = warp * 2 * R + (lane >> 4) * R;
-    const int c0 = (xw + MM) * AW + zl + MM;  // this lane's first cell pair in a P / Q tile
+    const int c0 = (xw + MM) * AW + zl + ZH;  // this lane's first cell pair in a P / Q tile
     T2 wp[R][8], wq[R][8];                    // P and Q at the last 8 planes, slot = item mod 8
     bool act[R], both = true;
     T cx1d[R], cx2[R];
@@ -113,7 +118,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     // the monopole enters the sweep's views of P and Q (..tti..:62-63)
     auto inject = [&](S *A, const Seg &s) {
         if (threadIdx.x == 0) {
-            const int at = (p.s_x - (s.x0 - MM)) * AW + (p.s_z - (s.z0 - MM));
+            const int at = (p.s_x - (s.x0 - MM)) * AW + (p.s_z - (s.z0 - ZH));
             A[at] = to_store<S, T>(ld<T>(A, at) + (T)p.amp0);
             A[L::H + at] = to_store<S, T>(ld<T>(A, L::H + at) + (T)p.amp1);
             fence_proxy_async();
@@ -127,18 +132,18 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             const bool zact = iz < p.nnz - MM;
             both = iz + 1 < p.nnz - MM;
             const int cza = min(iz, p.nnz - 1), czb = min(iz + 1, p.nnz - 1);
-            cz1d = T2{(T)p.cz1[cza] * (T)p.dtz, (T)p.cz1[czb] * (T)p.dtz};
+            cz1d = T2{scl<S>((T)p.cz1[cza] * (T)p.dtz, p.svp), scl<S>((T)p.cz1[czb] * (T)p.dtz, p.svp)};
             cz2 = T2{(T)p.cz2[cza], (T)p.cz2[czb]};
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int ix = s.x0 + xw + r;
                 act[r] = zact && ix < p.nnx - MM;
                 const int cxi = min(ix, p.nnx - 1);
-                cx1d[r] = (T)p.cx1[cxi] * (T)p.dtx;
+                cx1d[r] = scl<S>((T)p.cx1[cxi] * (T)p.dtx, p.svp);
                 cx2[r] = (T)p.cx2[cxi];
                 gb[r] = (uint32_t)iz + (uint32_t)p.ldz * (uint32_t)cxi;
             }
-            const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - MM);
+            const int lx = p.s_x - (s.x0 - MM), lz = p.s_z - (s.z0 - ZH);
             srcq = (p.inj && lx >= 0 && lx < L::AH && lz >= 0 && lz < AW) ? p.s_y : INT_MIN;
             cy1n = p.cy1[s.ya];
             cy2n = p.cy2[s.ya];
@@ -180,7 +185,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             const S *Ao = reinterpret_cast<const S *>(ringA + sh * L::A_STRIDE), *Bo = Ao + L::H;
             const S *Bu = reinterpret_cast<const S *>(sbp);
             const float *F = reinterpret_cast<const float *>(sbp + oF);
-            const T cy1d = (T)cy1n * (T)p.dty, cy2 = (T)cy2n;
+            const T cy1d = scl<S>((T)cy1n * (T)p.dty, p.svp), cy2 = (T)cy2n;
             cy1n = p.cy1[o + 1];  // o + 1 <= nny - 4: in bounds
             cy2n = p.cy2[o + 1];
             const uint32_t po = pstride * (uint32_t)o;
@@ -228,7 +233,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
 //                   px, py, pz, qx, qy, qz (core; only for tiles/planes on a damped axis)}
 template <int TX, class S, int D>
 struct TtiStrL {
-    static constexpr int AW = 40, AH = TX + 8;
+    static constexpr int AW = ZHalo<S>::W, AH = TX + 8;  // u / v / w tile [AH][AW], z halo ZH
     static constexpr uint32_t C = 32 * TX, H = AW * AH;
     static constexpr uint32_t A_BYTES = 3 * H * sizeof(S);  // u, v, w tiles
     static constexpr uint32_t B_FIXED = 2 * C * sizeof(S) + 7 * C * 4;
@@ -302,6 +307,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     using T = typename Arith<S>::T;
     using T2 = Two<T>;
     constexpr int NW = TX / (2 * R), AW = L::AW;
+    constexpr int ZS = WFieldZShift<S>::v;  // z offset of wavefield maps (2-byte storage)
+    constexpr int ZH = ZHalo<S>::ZH;        // first z cell of the tile inside a u / v / w row
     static_assert(NW >= 1, "a warp covers 2R tile rows");
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<typename L::Bars *>(smem + L::BAR_OFF);
@@ -332,19 +339,19 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 mbar_arrive_expect_tx(bar, L::A_BYTES + bbytes);
                 unsigned char *a = ringA + sa * L::A_STRIDE;
                 for (int k = 0; k < 3; ++k)
-                    tma_load_3d(a + k * L::H * sizeof(S), &mp.m[k], bar, s.z0 - MM, s.x0 - MM, q);
+                    tma_load_3d(a + k * L::H * sizeof(S), &mp.m[k], bar, s.z0 - ZH + ZS, s.x0 - MM, q);
                 if (!dst) return;
                 const int o = q - MM;
-                tma_load_3d(dst, &mp.m[3], bar, s.z0, s.x0, o);
-                tma_load_3d(dst + L::C * sizeof(S), &mp.m[4], bar, s.z0, s.x0, o);
+                tma_load_3d(dst, &mp.m[3], bar, s.z0 + ZS, s.x0, o);
+                tma_load_3d(dst + L::C * sizeof(S), &mp.m[4], bar, s.z0 + ZS, s.x0, o);
                 for (int k = 0; k < 7; ++k) tma_load_3d(dst + oF + k * L::C * 4, &mp.m[5 + k], bar, s.z0, s.x0, o);
                 unsigned char *ax = dst + oX;
                 const bool dm[3] = {range_damped(s.x0, TX, p.ulo[0], p.uhi[0]), range_damped(o, 1, p.ulo[1], p.uhi[1]),
                                     range_damped(s.z0, 32, p.ulo[2], p.uhi[2])};
                 for (int d = 0; d < 3; ++d)
                     if (dm[d]) {
-                        tma_load_3d(ax, &mp.m[12 + d], bar, s.z0, s.x0, o);
-                        tma_load_3d(ax + AUX, &mp.m[15 + d], bar, s.z0, s.x0, o);
+                        tma_load_3d(ax, &mp.m[12 + d], bar, s.z0 + ZS, s.x0, o);
+                        tma_load_3d(ax + AUX, &mp.m[15 + d], bar, s.z0 + ZS, s.x0, o);
                         ax += 2 * AUX;
                     }
             });
@@ -352,7 +359,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     }
 
     const int zl = 2 * (lane & 15), xw = warp * 2 * R + (lane >> 4) * R;
-    const int c0 = (xw + MM) * AW + zl + MM;  // this lane's first cell pair in a u / v / w tile
+    const int c0 = (xw + MM) * AW + zl + ZH;  // this lane's first cell pair in a u / v / w tile
     T2 wu[R][8], wv[R][8], ww[R][8];          // u, v, w at the last 8 planes, slot = item mod 8
     bool act[R], dxm[R], reca[R], recb[R], both = true, dza = false, dzb = false;
     float ax1[R], ax2[R];
@@ -364,7 +371,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     float ay1n = 1, ay2n = 1;
     const uint32_t pstride = (uint32_t)p.ldz * (uint32_t)p.nnx;
     const T k[4] = {(T)C8_0, (T)C8_1, (T)C8_2, (T)C8_3};
-    const T dtx = (T)p.dtx, dty = (T)p.dty, dtz = (T)p.dtz;
+    // 2-byte storage: P, Q hold sigma_P values, u, v, w sigma_v values
+    const T dtx = scl<S>((T)p.dtx, p.spv), dty = scl<S>((T)p.dty, p.spv), dtz = scl<S>((T)p.dtz, p.spv);
     pipe_run<TX, L::KA, L::KB, MM>(
         p.sw, w0, w1, bars, ringB, p.err,
         [&](const Seg &s) {
@@ -518,7 +526,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 }
                 if (o >= p.npml && o < p.npml + p.ny && (reca[r] | recb[r])) {  // ..tti..:313-323
                     const size_t tr = (size_t)trb[r] + (size_t)p.nx * (o - p.npml);
-                    T rr = reca[r] ? pa : pb;
+                    T rr = scl<S>(reca[r] ? pa : pb, p.rec_scale);
                     if (p.mute_nt && p.it < p.mute_nt[tr]) rr = T(0);
                     p.rec[tr * p.nt + p.it] = (float)rr;
                 }
@@ -547,10 +555,20 @@ static cudaError_t launch_tti_t(const K1Launch &L, cudaStream_t st) {
     return k1_launch(kern, NT, TtiStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, (S *)L.out1, p);
 }
 
+// 2-byte storage: tile widths 8 and 16, ring depths 0 and 2
+template <class S>
+static cudaError_t launch_tti_half(const K1Launch &L, cudaStream_t st) {
+    if (L.depth == 1) return cudaErrorInvalidConfiguration;
+    if (L.tx == 16) return L.depth ? launch_tti_t<16, S, 2, 1>(L, st) : launch_tti_t<16, S, 0, 1>(L, st);
+    return L.depth ? launch_tti_t<8, S, 2, 1>(L, st) : launch_tti_t<8, S, 0, 1>(L, st);
+}
+
 // configurations: (tile width, rows per lane) (8, 1), (16, 1), three ring depths
 cudaError_t launch_tti(const K1Launch &L, cudaStream_t st) {
     if (L.fp64) return launch_tti_t<8, double, 0, 1>(L, st);
     if (L.rows != 1) return cudaErrorInvalidConfiguration;
+    if (L.half == 1) return launch_tti_half<__nv_bfloat16>(L, st);
+    if (L.half == 2) return launch_tti_half<__half>(L, st);
     if (L.tx == 16)
         return L.depth == 2 ? launch_tti_t<16, float, 2, 1>(L, st)
              : L.depth == 1 ? launch_tti_t<16, float, 1, 1>(L, st)

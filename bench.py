@@ -57,10 +57,13 @@ STEP_BYTES = {"iso": 40.0, "2o": 16.0, "vti": 56.0, "tti": 60.0}
 #   unsplit step: (u, v, w, P) read and written at 2 B + 2 float parameters -> 24 B
 #   VTI: velocity P, Q, u, v, w (2 B) + 1/rho read, u, v, w written -> 20 B; stress
 #   u, v, w, P, Q (2 B) + rho, vp, eps, del read, P, Q written -> 30 B; step 36 B
-KERNEL_BYTES_2B = {"iso": (18.0, 18.0), "vti": (20.0, 30.0)}
+KERNEL_BYTES_2B = {"iso": (18.0, 18.0), "vti": (20.0, 30.0), "tti": (32.0, 42.0)}
 #   fused isotropic step (FP32): u, v, w, P, 1/rho, rho, vp read, u, v, w, P written -> 44 B
 FUSED_BYTES = 44.0
-STEP_BYTES_2B = {"iso": 24.0, "vti": 36.0}
+#   TTI: velocity P, Q, u, v, w (2 B) + 4 trig floats read, u, v, w written -> 32 B;
+#   stress u, v, w, P, Q (2 B) + vp, eps, del + 4 trig read, P, Q written -> 42 B;
+#   step: (u, v, w, P, Q) read and written at 2 B + 5 float parameters -> 40 B
+STEP_BYTES_2B = {"iso": 24.0, "vti": 36.0, "tti": 40.0}
 STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
 
 
@@ -383,8 +386,8 @@ def main():
         return
     cfgd, models, shot, meta = workload(args.workload, args.nt or None)
     meta["storage"] = args.storage
-    if args.storage != "fp32" and cfgd["physics"] not in ("iso", "vti"):
-        raise SystemExit("2-byte storage is built for the isotropic and VTI engines only")
+    if args.storage != "fp32" and cfgd["physics"] not in ("iso", "vti", "tti"):
+        raise SystemExit("2-byte storage is built for the 1st-order engines only")
     if args.impl == "reference":
         run_reference(args, cfgd, models, shot, meta)
         return

@@ -42,10 +42,11 @@ def test_invalid_config_rejected_without_gpu(engine_lib):
     assert "must be positive" in a3d.last_error()
 
 
-def test_half_storage_only_for_isotropic_and_vti(engine_lib):
-    """bfloat16 / float16 storage is built for the isotropic and VTI engines; others refuse it."""
+def test_half_storage_only_for_first_order_engines(engine_lib):
+    """bfloat16 / float16 storage is built for the isotropic, VTI and TTI engines; the
+    2nd-order engine refuses it."""
     import a3d
-    for phys in ("2o", "tti"):
+    for phys in ("2o",):
         cfg = a3d.make_config(phys, 10, 10, 10, storage=a3d.BF16)
         h = ctypes.c_void_p()
         rc = a3d.lib().a3d_engine_create(ctypes.byref(h), ctypes.byref(cfg), *[a3d._fptr(None)] * 6, 0)
