@@ -225,12 +225,6 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
 
     // 1st-order engines
     if ((rc = upload_model(e, vel, &e->vp, tmp))) return rc;
-    if (c.physics == A3D_ISO) {  // (rho * vp) * vp in float, the interior stress sweep's one coefficient
-        std::vector<float> pr(g.elems());
-        pad_model(rho, g, pr.data());
-        for (size_t i = 0; i < tmp.size(); ++i) pr[i] = (pr[i] * tmp[i]) * tmp[i];
-        if ((rc = upload_image(e, pr, &e->kfac))) return rc;
-    }
     if (c.physics != A3D_TTI) {
         if ((rc = upload_model(e, rho, &e->rho, tmp))) return rc;
         // the velocity sweeps multiply by 1/rho (float reciprocal); the padding is 0
@@ -360,12 +354,12 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
             (rc = mk(&mvel[2], e->v, true, BOX_CORE)) || (rc = mk(&mvel[3], e->w, true, BOX_CORE)) ||
             (rc = mk(&mvel[4], e->rinv, false, BOX_CORE)))
             return rc;
-        e->nstr = 10;
+        e->nstr = 9;
         if ((rc = mk(&mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&mstr[1], e->u, true, BOX_HX)) ||
             (rc = mk(&mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&mstr[3], e->P, true, BOX_CORE)) ||
             (rc = mk(&mstr[4], e->rho, false, BOX_CORE)) || (rc = mk(&mstr[5], e->vp, false, BOX_CORE)) ||
             (rc = mk(&mstr[6], e->px, true, BOX_CORE)) || (rc = mk(&mstr[7], e->py, true, BOX_CORE)) ||
-            (rc = mk(&mstr[8], e->pz, true, BOX_CORE)) || (rc = mk(&mstr[9], e->kfac, false, BOX_CORE)))
+            (rc = mk(&mstr[8], e->pz, true, BOX_CORE)))
             return rc;
         for (int b = 0; b < 2 && e->fused_ok; ++b) {  // fused step reading set b
             CUtensorMap *ms = e->mstep[t][b];

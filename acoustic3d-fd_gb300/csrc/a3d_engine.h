@@ -48,7 +48,6 @@ struct a3d_engine {
 
     // model parameters on the device (float, padded layout)
     float *vv = nullptr, *vp = nullptr, *rho = nullptr, *rinv = nullptr, *eps = nullptr, *del = nullptr;
-    float *kfac = nullptr;  // isotropic: (rho * vp) * vp, float (the interior stress coefficient)
     float *tct = nullptr, *tst = nullptr, *tcp = nullptr, *tsp = nullptr;  // TTI trig
     float v_mute = 0.0f;   // direct-wave mute velocity
 

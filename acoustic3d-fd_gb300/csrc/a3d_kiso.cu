@@ -12,7 +12,6 @@
 // the per-plane pipeline work is shared by R cells and the x-derivative reads
 // R + 7 tile rows instead of 8 R.
 #include <climits>
-#include <type_traits>
 
 #include "a3d_k1dev.cuh"
 
@@ -205,9 +204,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
 
 // ===========================================================================
 // iso_stress: maps {v (core), u (box HX), w (box HZ), P (core), rho, vp (core, float),
-//                   px, py, pz (core; loaded only for tiles/planes on a damped axis),
-//                   (rho vp) vp (core, float; interior items of float arithmetic load it
-//                   in place of rho and vp: the same float value, one field less)}
+//                   px, py, pz (core; loaded only for tiles/planes on a damped axis)}
 template <int TX, class S, int D>
 struct IsoStrL {
     static constexpr uint32_t C = 32 * TX;
@@ -228,7 +225,7 @@ struct IsoStrL {
 
 template <int TX, class S, int D, int R>
 __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
-    iso_stress(const __grid_constant__ Maps<10> mp, S *__restrict__ P,
+    iso_stress(const __grid_constant__ Maps<9> mp, S *__restrict__ P,
                const __grid_constant__ K1Params p) {
     using L = IsoStrL<TX, S, D>;
     using T = typename Arith<S>::T;
@@ -250,17 +247,9 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                      oX = L::B_FIXED;  // px, py, pz tiles follow the fixed part
     constexpr uint32_t AUX = L::AUX;
 
-    // interior items (tile and plane off the PML, no receiver row) of float arithmetic
-    // carry (rho vp) vp in the rho slot and no vp
-    constexpr bool KF = !std::is_same<S, double>::value;
-    auto interior = [&](const Seg &s, int o) {
-        return KF && !range_damped(s.x0, TX, p.ulo[0], p.uhi[0]) && !range_damped(s.z0, 32, p.ulo[2], p.uhi[2]) &&
-               !(p.npml >= s.z0 && p.npml < s.z0 + 32) && !range_damped(o, 1, p.ulo[1], p.uhi[1]);
-    };
-
     if (warp == NW) {  // producer warp: one thread issues every copy
         if (lane != 0) return;
-        for (int i = 0; i < 10; ++i) prefetch_tmap(&mp.m[i]);
+        for (int i = 0; i < 9; ++i) prefetch_tmap(&mp.m[i]);
         // split components only for tiles / planes on a damped axis, packed after the
         // fixed part in x, y, z order
         auto naux = [&](const Seg &s, int o) {
@@ -269,10 +258,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                    (uint32_t)range_damped(s.z0, 32, p.ulo[2], p.uhi[2]);
         };
         pipe_produce_m<TX, L::KA, L::KB, L::RB>(
-            p.sw, w0, w1, bars, ringB, p.err,
-            [&](const Seg &s, int o) {
-                return interior(s, o) ? (uint32_t)oV : L::B_FIXED + AUX * naux(s, o);
-            },
+            p.sw, w0, w1, bars, ringB, p.err, [&](const Seg &s, int o) { return L::B_FIXED + AUX * naux(s, o); },
             [&](uint32_t sa, unsigned char *dst, uint32_t bbytes, uint64_t *bar, const Seg &s, int q) {
                 mbar_arrive_expect_tx(bar, L::A_BYTES + bbytes);
                 tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0 + ZS, s.x0, q);
@@ -281,10 +267,6 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 tma_load_3d(dst, &mp.m[1], bar, s.z0 + ZS, s.x0 - MM, o);
                 tma_load_3d(dst + oW, &mp.m[2], bar, s.z0 - ZHalo<S>::ZH + ZS, s.x0, o);
                 tma_load_3d(dst + oP, &mp.m[3], bar, s.z0 + ZS, s.x0, o);
-                if (interior(s, o)) {
-                    tma_load_3d(dst + oR, &mp.m[9], bar, s.z0, s.x0, o);
-                    return;
-                }
                 tma_load_3d(dst + oR, &mp.m[4], bar, s.z0, s.x0, o);
                 tma_load_3d(dst + oV, &mp.m[5], bar, s.z0, s.x0, o);
                 unsigned char *ax = dst + oX;
@@ -415,20 +397,11 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                     const int bi = (xw + r) * 32 + zl;
                     T2 xx, zz;
                     deriv(r, xx, zz);
+                    const float2 rv = *reinterpret_cast<const float2 *>(Br + bi);
+                    const float2 vv = *reinterpret_cast<const float2 *>(Bvp + bi);
                     const T2 Po = ld2<T>(Bp, bi);
-                    // (((1 * rho) * vp) * vp) == (rho * vp) * vp  (..iso..:182-184), for float
-                    // arithmetic precomputed in float, so the value is the same
-                    T ta, tb;
-                    if constexpr (KF) {
-                        const float2 kk = *reinterpret_cast<const float2 *>(Br + bi);
-                        ta = kk.x;
-                        tb = kk.y;
-                    } else {
-                        const float2 rv = *reinterpret_cast<const float2 *>(Br + bi);
-                        const float2 vv = *reinterpret_cast<const float2 *>(Bvp + bi);
-                        ta = ((T)rv.x * (T)vv.x) * (T)vv.x;
-                        tb = ((T)rv.y * (T)vv.y) * (T)vv.y;
-                    }
+                    // (((1 * rho) * vp) * vp) == (rho * vp) * vp  (..iso..:182-184)
+                    const T ta = ((T)rv.x * (T)vv.x) * (T)vv.x, tb = ((T)rv.y * (T)vv.y) * (T)vv.y;
                     const T pa = ((Po.a - (ta * dtx) * xx.a) - (ta * dty) * yy[r].a) - (ta * dtz) * zz.a;
                     const T pb = ((Po.b - (tb * dtx) * xx.b) - (tb * dty) * yy[r].b) - (tb * dtz) * zz.b;
                     st2<S, T>(P, gb[r] + po, pa, pb);
@@ -515,8 +488,8 @@ static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
                          (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
     static bool attr = false;
-    Maps<10> mp;
-    for (int i = 0; i < 10; ++i) mp.m[i] = L.maps[i];
+    Maps<9> mp;
+    for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
     auto kern = iso_stress<TX, S, D, R>;
     const int grid = k1_sweep<TX>(p, kern, NT, IsoStrL<TX, S, D>::TOTAL, L.grid, L.mode);
     return k1_launch(kern, NT, IsoStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, p);

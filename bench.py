@@ -49,7 +49,11 @@ for _p in (PKG, os.path.join(ROOT, "oracle")):
 #   stress sweep:   read u, v, w, P, rho, vp; write P              -> 7 words
 # and the whole-step algorithmic figure of an unsplit formulation (u,v,w,P read and
 # written once + 2 parameters): 10 words = 40 B per cell update.
-KERNEL_BYTES = {"iso": (32.0, 28.0), "2o": (16.0, None), "vti": (40.0, 48.0), "tti": (56.0, 60.0)}
+#   VTI velocity: P, Q, u, v, w, 1/rho read, u, v, w written -> 9 words; stress: u, v, w,
+#   P, Q, rho, vp, eps, del read, P, Q written -> 11 words
+#   TTI velocity: P, Q, u, v, w + 4 trig read, u, v, w written -> 12 words; stress:
+#   u, v, w, P, Q, vp, eps, del + 4 trig read, P, Q written -> 14 words
+KERNEL_BYTES = {"iso": (32.0, 28.0), "2o": (16.0, None), "vti": (36.0, 44.0), "tti": (48.0, 56.0)}
 STEP_BYTES = {"iso": 40.0, "2o": 16.0, "vti": 56.0, "tti": 60.0}
 # 2-byte wavefield storage (isotropic and VTI engines; the model parameters stay float):
 #   velocity sweep: P, u, v, w (2 B) + 1/rho (4 B) read, u, v, w written -> 18 B
