@@ -9,7 +9,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <array>
+#include <map>
 #include <mutex>
+#include <string>
 
 #include "a3d_engine.h"
 
@@ -166,16 +169,52 @@ static int upload_image(a3d_engine *e, const std::vector<float> &img, float **ds
     return A3D_OK;
 }
 
-static int upload_model(a3d_engine *e, const float *m, float **dst, std::vector<float> &tmp) {
-    pad_model(m, e->g, tmp.data());
-    return upload_image(e, tmp, dst);
+// edge-replicated padding of a model on the device, the same clamp copy as pad_model
+// (zeros outside the field's cells); mode 1 stores 1 / value (0 where the value is 0),
+// mode 2 (value * s)^2
+__global__ void pad_field(const float *__restrict__ m, float *__restrict__ out, int nx, int ny, int nz, int pad,
+                          int nnx, int nny, int nnz, int ldz, size_t elems, int mode, float sc) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < elems; i += (size_t)gridDim.x * blockDim.x) {
+        float v = 0.0f;
+        if (i >= (size_t)Grid::zoff) {
+            const size_t f = i - Grid::zoff;
+            const int iz = (int)(f % ldz);
+            const size_t r = f / ldz;
+            const int ix = (int)(r % nnx), iy = (int)(r / nnx);
+            if (iz < nnz && iy < nny) {
+                const int cz = min(max(iz - pad, 0), nz - 1), cx = min(max(ix - pad, 0), nx - 1),
+                          cy = min(max(iy - pad, 0), ny - 1);
+                v = m[(size_t)cz + (size_t)nz * ((size_t)cx + (size_t)nx * cy)];
+                if (mode == 1) v = v != 0.0f ? 1.0f / v : 0.0f;
+                else if (mode == 2) { const float t = v * sc; v = t * t; }
+            }
+        }
+        out[i] = v;
+    }
+}
+
+// upload a model (nx*ny*nz host floats) into a new padded field; raw: a device
+// scratch buffer of the model's size
+static int upload_model(a3d_engine *e, const float *m, float **dst, float *raw, int mode = 0, float sc = 0.0f) {
+    const Grid &g = e->g;
+    *dst = (float *)e->dfield(4);
+    if (!*dst) return fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", e->field_bytes(4));
+    CUDA_TRY(cudaMemcpy(raw, m, (size_t)g.nx * g.ny * g.nz * 4, cudaMemcpyHostToDevice));
+    pad_field<<<1024, 256>>>(raw, (float *)e->field_alloc(*dst, 4), g.nx, g.ny, g.nz, g.pad, g.nnx, g.nny, g.nnz,
+                             g.ldz, g.elems(), mode, sc);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaDeviceSynchronize());
+    return A3D_OK;
 }
 
 static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const float *eps,
                         const float *del, const float *theta, const float *phi) {
     const a3d_config &c = e->cfg;
     const Grid &g = e->g;
-    std::vector<float> tmp(g.elems());
+    std::vector<float> tmp;
+    float *raw = nullptr;  // device scratch for one model array
+    CUDA_TRY(cudaMalloc(&raw, (size_t)c.nx * c.ny * c.nz * 4));
+    struct FreeRaw { float *p; ~FreeRaw() { cudaFree(p); } } free_raw{raw};
     const size_t fb = g.elems() * e->esz;
     auto field = [&](void **p) -> int {
         *p = e->dfield(e->esz);
@@ -189,12 +228,7 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
 
     if (c.physics == A3D_2ORDER) {
         // vv = (v dt)^2 on the padded grid (Toa_3dfd_cuda.cu:300-347)
-        pad_model(vel, g, tmp.data());
-        for (size_t i = 0; i < tmp.size(); ++i) {
-            const float t = tmp[i] * c.dt;
-            tmp[i] = t * t;
-        }
-        if ((rc = upload_image(e, tmp, &e->vv))) return rc;
+        if ((rc = upload_model(e, vel, &e->vv, raw, 2, c.dt))) return rc;
         e->v_mute = (size_t)c.nx * c.ny * c.nz > 1 ? vel[1] : vel[0];  // 2O:403
         if ((rc = field(&e->X)) || (rc = field(&e->Y))) return rc;
         // sponge factors per axis
@@ -224,19 +258,19 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     }
 
     // 1st-order engines
-    if ((rc = upload_model(e, vel, &e->vp, tmp))) return rc;
+    if ((rc = upload_model(e, vel, &e->vp, raw))) return rc;
     if (c.physics != A3D_TTI) {
-        if ((rc = upload_model(e, rho, &e->rho, tmp))) return rc;
+        if ((rc = upload_model(e, rho, &e->rho, raw))) return rc;
         // the velocity sweeps multiply by 1/rho (float reciprocal); the padding is 0
-        for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = tmp[i] != 0.0f ? 1.0f / tmp[i] : 0.0f;
-        if ((rc = upload_image(e, tmp, &e->rinv))) return rc;
+        if ((rc = upload_model(e, rho, &e->rinv, raw, 1))) return rc;
     }
     if (c.physics != A3D_ISO) {
-        if ((rc = upload_model(e, eps, &e->eps, tmp))) return rc;
-        if ((rc = upload_model(e, del, &e->del, tmp))) return rc;
+        if ((rc = upload_model(e, eps, &e->eps, raw))) return rc;
+        if ((rc = upload_model(e, del, &e->del, raw))) return rc;
     }
     if (c.physics == A3D_TTI) {
-        // cos/sin of tilt and azimuth in float, as ..tti..:101-103 evaluates them
+        // cos/sin of tilt and azimuth in float on the host, as ..tti..:101-103 evaluates them
+        tmp.resize(g.elems());
         std::vector<float> ang(g.elems());
         float **dst[4] = {&e->tct, &e->tst, &e->tcp, &e->tsp};
         for (int k = 0; k < 4; ++k) {
@@ -441,25 +475,55 @@ static int check_kernel_error(a3d_engine *e) {
 // stress) and the fused sweep.  Unless A3D_FUSED or a pinned A3D_TUNE decides, both
 // are tuned and the faster one (summed launch times of the two sweeps against the
 // fused step's) runs.
+// Tuned launch shapes are remembered per process for each (device, physics,
+// storage, padded grid, absorber, step forms, tile request), so engines made again
+// for the same grid — a3d_forward_host calls, shots on equal windows — skip the tuner.
+static std::mutex g_tune_mu;
+static std::map<std::string, std::pair<std::array<a3d_engine::Tune, 2>, bool>> g_tune_cache;
+
 int a3d_engine::autotune() {
     const char *fz = getenv("A3D_FUSED"), *pin = getenv("A3D_TUNE");
     const bool forced = fz && (fz[0] == '0' || fz[0] == '1');
-    if (!fused_ok || forced || (pin && *pin && !fp64)) {
+    if (forced || (pin && *pin && !fp64)) {
         fused = fused_ok && fz && fz[0] == '1';
         return autotune_form();
+    }
+    char key[256];
+    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", device, cfg.physics, cfg.storage, g.nnz, g.nnx, g.nny,
+             npml, (int)learned, (int)fused_ok, cfg.tile_x);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            tune[0] = it->second.first[0];
+            tune[1] = it->second.first[1];
+            tuned = true;
+            if (it->second.second && fused_ok) {
+                fused = true;
+                return A3D_OK;
+            }
+            return drop_fused();
+        }
     }
     fused = false;
     int rc = autotune_form();
     if (rc) return rc;
+    if (!fused_ok) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = {{tune[0], tune[1]}, false};
+        return A3D_OK;
+    }
     const Tune two[2] = {tune[0], tune[1]};
     fused = true;
     if ((rc = autotune_form())) return rc;
     if (tune[0].ms >= two[0].ms + two[1].ms) {
         tune[0] = two[0];
         tune[1] = two[1];
-        return drop_fused();
+        rc = drop_fused();
     }
-    return A3D_OK;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = {{tune[0], tune[1]}, fused};
+    return rc;
 }
 
 // run the two-sweep form from now on; the second buffer set only serves the fused
@@ -938,6 +1002,7 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
     if (device < 0 || device >= ndev) return fail(A3D_E_ARG, "device %d not present (%d devices)", device, ndev);
     CUDA_TRY(cudaSetDevice(device));
     CUDA_TRY(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, device));
+    cudaGetLastError();  // a refused launch configuration of an earlier engine leaves nothing pending here
     a3d_engine *e = new (std::nothrow) a3d_engine;
     if (!e) return fail(A3D_E_NOMEM, "host allocation failed");
     e->cfg = *cfg;

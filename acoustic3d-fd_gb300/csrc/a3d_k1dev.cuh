@@ -38,8 +38,12 @@ static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid,
     p.sw.y_begin = MM;
     p.sw.NY = p.nny - 2 * MM;
     int occ = 0;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nthreads, smem);
+    // a ring larger than a CTA's shared memory is refused by k1_launch; do not let the
+    // attribute call fail here and leave its error pending for a later launch check
+    if (smem_fits(smem)) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nthreads, smem);
+    }
     const int g = plan_sweep(p.sw, occ, mode);
     return grid > 0 ? grid : g;
 }
