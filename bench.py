@@ -21,7 +21,7 @@ A "step" is one shot: the full nt-step time loop over the padded grid.
          FP64 (GPU FP64 path), outside the timed region
 
 --impl reference runs the reference's update restated on the CPU (the reference
-itself is CUDA-only; its kernels' GPU timing is reported in the design doc).
+itself is CUDA-only; oracle/time_reference.py times its kernels on the GPU).
 Multi-GPU: replicas (torchrun; each rank runs its own shots, no collective in the
 data path); value = all ranks' updates / max rank time.
 """

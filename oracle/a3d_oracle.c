@@ -1,8 +1,8 @@
 /*
  * a3d_oracle.c — CPU restatement of the reference forward-modelling engines.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA engines (tests, smoke check,
- * CPU-baseline leg of the benchmark).  The product path never uses it.
+ * TEST INFRASTRUCTURE ONLY: the oracle the CUDA engines are tested against (tests,
+ * smoke check, CPU-baseline leg of the benchmark).  The product path never uses it.
  *
  * Setup pieces (padding, wavelets, PML profiles, direct-wave mute) live here and
  * are shared by both precisions; the time loops are in a3d_oracle_loops.inc,

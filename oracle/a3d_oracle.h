@@ -1,9 +1,9 @@
 /*
  * a3d_oracle.h — CPU restatement of the reference forward-modelling engines.
  *
- * TEST INFRASTRUCTURE ONLY.  These functions are the checker for the CUDA
- * engines: the tests, the smoke check and the CPU-baseline leg of the benchmark
- * call them.  The product path never links, loads or calls them.
+ * TEST INFRASTRUCTURE ONLY.  These functions are the oracle the CUDA engines are
+ * tested against: the tests, the smoke check and the CPU-baseline leg of the
+ * benchmark call them.  The product path never links, loads or calls them.
  *
  * Each engine runs one shot on the host, OpenMP-parallel over y-planes, and
  * returns the full (undecimated) receiver record in the reference's internal

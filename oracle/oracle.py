@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/a3d_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` as the checker.  The product never imports it.
+CPU-baseline leg of ``bench.py`` as the oracle.  The product never imports it.
 
 The oracle restates the reference engines (paths relative to the reference
 project): src/Toa_3dfd_cuda.cu (2nd order), src/Toa_gpu_3diso_fd_1orderfunciton.cu

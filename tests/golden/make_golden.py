@@ -5,7 +5,7 @@ kernels were built into oracle/_ref/ by oracle/build_ref.sh (on a machine that
 has the reference sources):
 
     make -C oracle harness
-    python tests/golden/make_golden.py --out gpurun_out/golden
+    python tests/golden/make_golden.py --out /tmp/golden
 
 Each case seeds a small smooth model (numpy default_rng + Gaussian smoothing),
 writes it in the reference's raw float32 format, runs the reference's own CUDA

@@ -1,7 +1,7 @@
 """The CUDA engines against the reference's own CUDA kernels (golden records).
 
 Gate: shot-record relative L2 <= 1e-5 for the FP32 path on the unmuted record
-(the spec parity gate); the muted record must zero exactly the samples the
+(the project's parity gate); the muted record must zero exactly the samples the
 reference zeroed.
 """
 import numpy as np
