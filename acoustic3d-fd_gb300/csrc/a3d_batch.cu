@@ -7,6 +7,8 @@
 // consecutive shots use the same window, and carries the tuned launch shapes
 // over to the engines of later windows.
 #include <cstring>
+#include <functional>
+#include <thread>
 #include <vector>
 
 #include "a3d_engine.h"
@@ -21,8 +23,7 @@ bool same_window(const a3d_window &a, const a3d_window &b) {
 
 // the window [x0, x0+nx) x [y0, y0+ny) x [z0, z0+nz) of a model array (z fastest,
 // then x, then y) as a dense array of the same order
-void crop(const float *m, const a3d_config &c, const a3d_window &w, std::vector<float> &out) {
-    out.resize((size_t)w.nx * w.ny * w.nz);
+void crop(const float *m, const a3d_config &c, const a3d_window &w, float *out) {
     for (int iy = 0; iy < w.ny; ++iy)
         for (int ix = 0; ix < w.nx; ++ix)
             memcpy(&out[((size_t)iy * w.nx + ix) * w.nz],
@@ -67,13 +68,30 @@ extern "C" int a3d_run_batch(const a3d_problem *pb, const a3d_shot *shots, int n
             wc.ny = w.ny;
             wc.nz = w.nz;
             const float *wa[6];
-            for (int k = 0; k < 6; ++k) {
+            std::vector<std::thread> ts;  // one host thread per model array to crop
+            bool oom = false;
+            for (int k = 0; k < 6 && !oom; ++k) {
                 if (!arrays[k] || same_window(w, whole)) {
                     wa[k] = arrays[k];
                     continue;
                 }
-                crop(arrays[k], c, w, cropped[k]);
+                try {
+                    cropped[k].resize((size_t)w.nx * w.ny * w.nz);
+                } catch (...) {
+                    oom = true;
+                    break;
+                }
                 wa[k] = cropped[k].data();
+                try {
+                    ts.emplace_back(crop, arrays[k], std::cref(c), std::cref(w), cropped[k].data());
+                } catch (...) {  // no thread: crop here
+                    crop(arrays[k], c, w, cropped[k].data());
+                }
+            }
+            for (auto &t : ts) t.join();
+            if (oom) {
+                rc = fail(A3D_E_NOMEM, "host allocation of a %dx%dx%d window failed", w.nx, w.ny, w.nz);
+                break;
             }
             rc = a3d_engine_create(&e, &wc, wa[0], wa[1], wa[2], wa[3], wa[4], wa[5], o->device);
             if (rc) break;

@@ -13,6 +13,8 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "a3d_engine.h"
 
@@ -161,15 +163,8 @@ void *a3d_engine::dfield(size_t es) {
     return p ? p + Grid::zoff * es : nullptr;
 }
 
-// copy a host image of a float field allocation (elems() floats) into a new field
-static int upload_image(a3d_engine *e, const std::vector<float> &img, float **dst) {
-    *dst = (float *)e->dfield(4);
-    if (!*dst) return fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", e->field_bytes(4));
-    CUDA_TRY(cudaMemcpy(e->field_alloc(*dst, 4), img.data(), e->field_bytes(4), cudaMemcpyHostToDevice));
-    return A3D_OK;
-}
-
-// edge-replicated padding of a model on the device, the same clamp copy as pad_model
+// edge-replicated padding of a model on the device: the reference's three one-axis
+// copies (..iso..:198-260 pad_vv) compose to a clamp of each index into the model
 // (zeros outside the field's cells); mode 1 stores 1 / value (0 where the value is 0),
 // mode 2 (value * s)^2
 __global__ void pad_field(const float *__restrict__ m, float *__restrict__ out, int nx, int ny, int nz, int pad,
@@ -205,6 +200,29 @@ static int upload_model(a3d_engine *e, const float *m, float **dst, float *raw, 
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaDeviceSynchronize());
     return A3D_OK;
+}
+
+// out[i] = cosf(a[i]) (sine: sinf) for n values, split over the host's threads
+static void host_trig(const float *a, float *out, size_t n, bool sine) {
+    auto part = [=](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) out[i] = sine ? sinf(a[i]) : cosf(a[i]);
+    };
+    size_t nth = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 32);
+    nth = std::min(nth, n / 65536 + 1);
+    std::vector<std::thread> ts;
+    const size_t chunk = (n + nth - 1) / nth;
+    size_t next = std::min(n, chunk);  // this thread takes [0, chunk); threads take the rest
+    try {
+        while (next < n) {
+            const size_t hi = std::min(n, next + chunk);
+            ts.emplace_back(part, next, hi);
+            next = hi;
+        }
+    } catch (...) {  // a thread could not be started: this thread computes what is left
+    }
+    part(0, std::min(n, chunk));
+    if (next < n) part(next, n);
+    for (auto &t : ts) t.join();
 }
 
 static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const float *eps,
@@ -269,14 +287,16 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
         if ((rc = upload_model(e, del, &e->del, raw))) return rc;
     }
     if (c.physics == A3D_TTI) {
-        // cos/sin of tilt and azimuth in float on the host, as ..tti..:101-103 evaluates them
-        tmp.resize(g.elems());
-        std::vector<float> ang(g.elems());
+        // cos/sin of tilt and azimuth in float on the host (libm, as the oracle and
+        // ..tti..:101-103 evaluate them), on the model cells over host threads, then
+        // padded on the device like every model array: edge replication commutes
+        // with a pointwise function, so every grid cell gets the value of cos / sin
+        // of its padded angle
+        tmp.resize((size_t)c.nx * c.ny * c.nz);
         float **dst[4] = {&e->tct, &e->tst, &e->tcp, &e->tsp};
         for (int k = 0; k < 4; ++k) {
-            pad_model(k < 2 ? theta : phi, g, ang.data());
-            for (size_t i = 0; i < ang.size(); ++i) tmp[i] = (k % 2 == 0) ? cosf(ang[i]) : sinf(ang[i]);
-            if ((rc = upload_image(e, tmp, dst[k]))) return rc;
+            host_trig(k < 2 ? theta : phi, tmp.data(), tmp.size(), k % 2 == 1);
+            if ((rc = upload_model(e, tmp.data(), dst[k], raw))) return rc;
         }
     }
     // mute velocity: the padded model's element 1, i.e. model cell (0,0,0) (..iso..:340)

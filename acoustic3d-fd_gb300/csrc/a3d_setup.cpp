@@ -10,26 +10,6 @@ namespace a3d {
 
 static const double PI_REF = 3.141592653;  // the reference's pi / PI macro (2O:14, ISO:28)
 
-void pad_model(const float *m, const Grid &g, float *out) {
-    for (size_t i = 0; i < g.elems(); ++i) out[i] = 0.0f;
-    out += Grid::zoff;
-    for (int iy = 0; iy < g.nny; ++iy) {
-        int cy = iy - g.pad;
-        cy = cy < 0 ? 0 : (cy >= g.ny ? g.ny - 1 : cy);
-        for (int ix = 0; ix < g.nnx; ++ix) {
-            int cx = ix - g.pad;
-            cx = cx < 0 ? 0 : (cx >= g.nx ? g.nx - 1 : cx);
-            const float *src = m + ((size_t)cy * g.nx + cx) * g.nz;
-            float *dst = out + g.idx(0, ix, iy);
-            for (int iz = 0; iz < g.nnz; ++iz) {
-                int cz = iz - g.pad;
-                cz = cz < 0 ? 0 : (cz >= g.nz ? g.nz - 1 : cz);
-                dst[iz] = src[cz];
-            }
-        }
-    }
-}
-
 float ricker2o(int it, float dt, float fm) {
     const float a = (float)it * dt;                    // it*dt in float
     const double d = (double)a - 1.0 / (double)fm;     // - 1.0/fm in double

@@ -28,11 +28,6 @@ struct Grid {
     }
 };
 
-// Edge-replicated copy of a model (z fastest, x, y) into a host image of a field
-// allocation (elems() floats; the field base sits zoff elements in); the
-// reference's three one-axis copies compose to a clamp.
-void pad_model(const float *m, const Grid &g, float *out);
-
 float ricker2o(int it, float dt, float fm);          // Toa_3dfd_cuda.cu:34-43
 float wavelet1(int wtype, float t, float favg);      // ..iso..:52-87
 float pml_d0(float vmid, int npml, float dx, float dy, float dz);  // ..iso..:193-195
