@@ -189,12 +189,12 @@ __global__ void pad_field(const float *__restrict__ m, float *__restrict__ out, 
 }
 
 // upload a model (nx*ny*nz host floats) into a new padded field; raw: a device
-// scratch buffer of the model's size
+// scratch buffer of the model's size; m == nullptr pads what raw already holds
 static int upload_model(a3d_engine *e, const float *m, float **dst, float *raw, int mode = 0, float sc = 0.0f) {
     const Grid &g = e->g;
     *dst = (float *)e->dfield(4);
     if (!*dst) return fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", e->field_bytes(4));
-    CUDA_TRY(cudaMemcpy(raw, m, (size_t)g.nx * g.ny * g.nz * 4, cudaMemcpyHostToDevice));
+    if (m) CUDA_TRY(cudaMemcpy(raw, m, (size_t)g.nx * g.ny * g.nz * 4, cudaMemcpyHostToDevice));
     pad_field<<<1024, 256>>>(raw, (float *)e->field_alloc(*dst, 4), g.nx, g.ny, g.nz, g.pad, g.nnx, g.nny, g.nnz,
                              g.ldz, g.elems(), mode, sc);
     CUDA_TRY(cudaGetLastError());
@@ -279,8 +279,8 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     if ((rc = upload_model(e, vel, &e->vp, raw))) return rc;
     if (c.physics != A3D_TTI) {
         if ((rc = upload_model(e, rho, &e->rho, raw))) return rc;
-        // the velocity sweeps multiply by 1/rho (float reciprocal); the padding is 0
-        if ((rc = upload_model(e, rho, &e->rinv, raw, 1))) return rc;
+        // the velocity sweeps multiply by 1/rho (float reciprocal) of the rho just uploaded
+        if ((rc = upload_model(e, nullptr, &e->rinv, raw, 1))) return rc;
     }
     if (c.physics != A3D_ISO) {
         if ((rc = upload_model(e, eps, &e->eps, raw))) return rc;

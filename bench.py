@@ -485,10 +485,13 @@ def main():
     e.close()
 
     # ---- e2e through the host-buffer C-ABI call (H2D model, loop, D2H record)
-    n_model = len(a3d.READS[cfg.physics])
+    # model arrays copied to the device per call, unpadded (padding runs on the device):
+    # 2O v; ISO v, rho; VTI v, rho, epsilon, delta; TTI v, epsilon, delta and the host's
+    # cos / sin of tilt and azimuth
+    n_upload = {"2o": 1, "iso": 2, "vti": 4, "tti": 7}[eng]
     pad = cfgd["npml"] + (4 if eng == "2o" else 0)
     padded = (cfgd["nx"] + 2 * pad) * (cfgd["ny"] + 2 * pad) * ((cfgd["nz"] + 2 * pad + 7) // 8 * 8)
-    h2d = 4 * padded * n_model
+    h2d = 4 * cfgd["nx"] * cfgd["ny"] * cfgd["nz"] * n_upload
     d2h = 4 * cfgd["nx"] * cfgd["ny"] * cfgd["nt"]
     e2e_val = None
     if args.e2e_steps > 0:
