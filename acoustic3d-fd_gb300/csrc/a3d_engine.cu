@@ -194,7 +194,10 @@ static int upload_model(a3d_engine *e, const float *m, float **dst, float *raw, 
     const Grid &g = e->g;
     *dst = (float *)e->dfield(4);
     if (!*dst) return fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", e->field_bytes(4));
-    if (m) CUDA_TRY(cudaMemcpy(raw, m, (size_t)g.nx * g.ny * g.nz * 4, cudaMemcpyHostToDevice));
+    if (m) {
+        const int r = stage_to_device(raw, m, (size_t)g.nx * g.ny * g.nz * 4, e->st);
+        if (r) return r;
+    }
     pad_field<<<1024, 256>>>(raw, (float *)e->field_alloc(*dst, 4), g.nx, g.ny, g.nz, g.pad, g.nnx, g.nny, g.nnz,
                              g.ldz, g.elems(), mode, sc);
     CUDA_TRY(cudaGetLastError());

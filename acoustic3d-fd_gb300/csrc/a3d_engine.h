@@ -15,6 +15,10 @@ namespace a3d {
 int fail(int code, const char *fmt, ...);
 void clear_error();
 
+// copy of a large pageable host buffer to the device through a pinned staging ring
+// (a3d_stage.cu); waits for the copy (stream st) and returns an A3D_* code
+int stage_to_device(void *dst, const void *src, size_t bytes, cudaStream_t st);
+
 // tensor map over a padded field (dims nnz, nnx, nny; rows of g.ldz elements)
 // dtype: 0 float, 1 bfloat16, 2 float16, 3 double
 int make_field_map(CUtensorMap *m, const void *base, int dtype, const Grid &g, int box0, int box1);

@@ -10,9 +10,11 @@ runs at the 256^3, 2000-step size of the isotropic benchmark:
 * An isotropic shot in a model that depends on depth only, with the source on the
   x = y diagonal and dx = dy, is symmetric under the swap of x and y.  The two
   orders of the pressure update's x and y terms round differently, so the record
-  and its transpose agree to float rounding (rel-L2 1e-5), not bit for bit.
+  and its transpose agree to float rounding (rel-L2 below 1e-5; measured 1.1e-6),
+  not bit for bit.
 * In a homogeneous medium the delay between the traces of two receivers is their
-  difference in distance from the source over the velocity.
+  difference in distance from the source over the velocity (within 1 ms; measured
+  0.15 ms off on a 49 ms delay).
 * The PML takes the energy out: once the wave has left the model, the pressure
   energy inside it is a tiny fraction of its peak.
 """
@@ -90,10 +92,10 @@ def test_homogeneous_moveout_is_distance_over_velocity(engine_lib):
     h = 41 * d  # depth of the dipole's centre below the receivers (model z = 0)
     r1, r2 = h, np.hypot(h, off * d)
     lag = _lag_seconds(rec[iy0, ix0], rec[iy0, ix0 + off], dt)
-    assert abs(lag - (r2 - r1) / vp) < 2e-3, (lag, (r2 - r1) / vp)
+    assert abs(lag - (r2 - r1) / vp) < 1e-3, (lag, (r2 - r1) / vp)
     # the same along y
     lag_y = _lag_seconds(rec[iy0, ix0], rec[iy0 + off, ix0], dt)
-    assert abs(lag_y - (r2 - r1) / vp) < 2e-3, (lag_y, (r2 - r1) / vp)
+    assert abs(lag_y - (r2 - r1) / vp) < 1e-3, (lag_y, (r2 - r1) / vp)
 
 
 def test_pml_takes_the_energy_out(engine_lib):
@@ -109,5 +111,6 @@ def test_pml_takes_the_energy_out(engine_lib):
     energy = (snaps.astype(np.float64) ** 2).reshape(len(snaps), -1).sum(axis=1)
     peak = energy.max()
     assert peak > 0
-    # the wave crosses the 640 m model in 0.32 s; by 1.15 s it has left it
-    assert energy[-1] < 1e-4 * peak, energy[-1] / peak
+    # the wave crosses the 640 m model in 0.32 s; by 1.15 s it has left it (measured
+    # on a GB300: 3e-10 of the peak)
+    assert energy[-1] < 1e-6 * peak, energy[-1] / peak
