@@ -464,11 +464,18 @@ def main():
         kname = "iso_step"
     meta["fused_step"] = bool(desc.get("fused"))
     tr = traffic_per_launch(meta["workload"] + ("" if args.storage == "fp32" else "_" + args.storage))
+    traffic = tr.get(kname) if isinstance(tr, dict) else None
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": tr.get(kname) if isinstance(tr, dict) else None,
+                "frac": achieved / peak, "traffic": traffic,
                 "peak_source": peak_kind, "bytes_per_cell": kb[dom],
                 "kernel_ms_per_launch": per[dom],
                 "step": {"bytes_per_cell": step_b, "achieved": step_gbs, "frac": step_gbs / peak}}
+    if traffic and per[dom] > 0:
+        # the DRAM bytes ncu measured for one launch of this kernel over this run's
+        # event-timed launch: how fast the kernel actually draws from HBM, PML split
+        # components and halo re-reads included
+        roofline["traffic_gbs"] = traffic / (per[dom] / 1000.0) / 1e9
+        roofline["traffic_frac"] = roofline["traffic_gbs"] / peak
 
     # ---- FP64 error of the FP32 record (outside the timed region)
     rel = None
