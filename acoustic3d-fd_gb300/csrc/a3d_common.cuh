@@ -183,6 +183,10 @@ struct Sweep {
     int NY;          // output planes per tile
     int Yc;          // planes per y chunk
     long long W;     // ntz * ntx * NY
+    // 1: column (chunk c, x tile xt) visits its z tiles rotated by
+    // ntz * (c * ntx + xt) / (chunks * ntx), so CTAs far apart in the sweep (those that
+    // share an SM) start from different z tiles
+    int rot;
 };
 
 __device__ __forceinline__ void cta_range(const Sweep &s, long long &w0, long long &w1) {

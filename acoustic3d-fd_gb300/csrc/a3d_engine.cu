@@ -580,19 +580,25 @@ int a3d_engine::autotune_form() {
     else shapes = {{8, 1}, {16, 1}};
     if (fused) shapes = {{8, 1}, {16, 1}, {8, 2}, {16, 2}};  // the fused step: ring depths 0 and 1
     const int maxdepth = fused ? 1 : 2;
-    // A3D_TUNE="tx,rows,depth,plan[;tx,rows,depth,plan]" pins the launch configuration of
-    // each kernel kind (velocity; stress) instead of timing candidates
+    // A3D_TUNE="tx,rows,depth,plan[,rot][;tx,rows,depth,plan[,rot]]" pins the launch
+    // configuration of each kernel kind (velocity; stress) instead of timing candidates
     if (const char *env = getenv("A3D_TUNE"); env && *env && !fp64) {
         const char *q = env;
         for (int k = 0; k < 2; ++k) {
-            int tx = 0, rows = 0, depth = 0, mode = 0, n = 0;
+            int tx = 0, rows = 0, depth = 0, mode = 0, n = 0, rot = 0, n2 = 0;
             if (sscanf(q, "%d,%d,%d,%d%n", &tx, &rows, &depth, &mode, &n) != 4 || (tx != 8 && tx != 16) ||
                 depth < 0 || depth > maxdepth || (fused && rows == 4) ||
                 (rows != 1 && rows != 2 && rows != 4) || (rows == 4 && tx != 16) || mode < 0 || mode > 1)
-                return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[;...], got \"%s\"", env);
+                return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[,rot][;...], got \"%s\"", env);
+            if (q[n] == ',') {
+                if (sscanf(q + n + 1, "%d%n", &rot, &n2) != 1 || rot < 0 || rot > 1)
+                    return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[,rot][;...], got \"%s\"", env);
+                n += 1 + n2;
+            }
             if (!multirow && rows != 1) return fail(A3D_E_ARG, "A3D_TUNE: this physics runs one row per warp");
             tune[k] = Tune{tx, depth, mode, rows};
             tune[k].ms = 0;
+            tune[k].rot = c.physics == A3D_2ORDER ? 0 : rot;
             q += n;
             if (*q == ';') ++q;
             else if (k == 0) { tune[1] = tune[0]; break; }
@@ -614,7 +620,9 @@ int a3d_engine::autotune_form() {
     CUDA_TRY(cudaEventCreate(&t1));
     for (int k = 0; k < kinds; ++k) {
         float best = 1e30f;
-        for (const Tune &tc : cand) {
+        // ms per launch of candidate tc (one warm-up, three timed); f < 0: it does not run
+        auto time_cand = [&](const Tune &tc, float &f) -> int {
+            f = -1.0f;
             const int ti = tc.tx == 16 ? 1 : 0;
             auto launch_once = [&]() -> cudaError_t {
                 if (c.physics == A3D_2ORDER) {
@@ -652,6 +660,7 @@ int a3d_engine::autotune_form() {
                 L.out0 = k == 0 ? u : P; L.out1 = k == 0 ? v : Q; L.out2 = w;
                 L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
                 L.half = half;
+                L.rot = tc.rot;
                 p.svp = p.spv = p.rec_scale = 1.0f;
                 if (fused) {  // set 0 read, set 1 written
                     L.kind = K1_ISO_STEP;
@@ -663,22 +672,40 @@ int a3d_engine::autotune_form() {
                 auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
                 return launch(L, st);
             };
-            if (launch_once() != cudaSuccess) { cudaGetLastError(); continue; }
+            if (launch_once() != cudaSuccess) { cudaGetLastError(); return A3D_OK; }
             CUDA_TRY(cudaEventRecord(t0, st));
             bool ok = true;
             for (int r = 0; r < 3 && ok; ++r) ok = launch_once() == cudaSuccess;
             CUDA_TRY(cudaEventRecord(t1, st));
             CUDA_TRY(cudaEventSynchronize(t1));
-            if (!ok) { cudaGetLastError(); continue; }
-            float f = 0;
-            CUDA_TRY(cudaEventElapsedTime(&f, t0, t1));
-            if (f < best) {
+            if (!ok) { cudaGetLastError(); return A3D_OK; }
+            float e3 = 0;
+            CUDA_TRY(cudaEventElapsedTime(&e3, t0, t1));
+            f = e3 / 3;
+            return A3D_OK;
+        };
+        for (const Tune &tc : cand) {
+            float f = -1.0f;
+            const int rt = time_cand(tc, f);
+            if (rt) return rt;
+            if (f >= 0.0f && f < best) {
                 best = f;
                 tune[k] = tc;
-                tune[k].ms = f / 3;
+                tune[k].ms = f;
             }
         }
         if (best >= 1e30f) return fail(A3D_E_CUDA, "no launch configuration of kernel kind %d runs", k);
+        if (c.physics != A3D_2ORDER && !fp64) {  // the chosen shape with the rotated z-tile order
+            Tune r = tune[k];
+            r.rot = 1;
+            float f = -1.0f;
+            const int rt = time_cand(r, f);
+            if (rt) return rt;
+            if (f >= 0.0f && f < tune[k].ms) {
+                tune[k] = r;
+                tune[k].ms = f;
+            }
+        }
     }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
@@ -889,6 +916,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         Ls.out0 = P; Ls.out1 = Q;
         Lv.tx = tune[0].tx; Lv.depth = tune[0].depth; Lv.mode = tune[0].mode; Lv.rows = tune[0].rows;
         Ls.tx = tune[1].tx; Ls.depth = tune[1].depth; Ls.mode = tune[1].mode; Ls.rows = tune[1].rows;
+        Lv.rot = tune[0].rot; Ls.rot = tune[1].rot;
         Lv.fp64 = Ls.fp64 = fp64; Lv.half = Ls.half = half; Lv.grid = Ls.grid = 0;
         auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
         if (learned && !cl_packed) return fail(A3D_E_ARG, "learned rim without a closure (a3d_engine_set_closure)");
@@ -1225,11 +1253,11 @@ extern "C" int a3d_engine_describe(a3d_engine *e, char *buf, size_t n) {
     }
     snprintf(buf, n,
              "{\"grid\": [%d, %d, %d], \"ldz\": %d, \"pad\": %d, \"device_bytes\": %zu, \"fused\": %d, "
-             "\"kernels\": [{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"ms\": %.4f}, "
-             "{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"ms\": %.4f}]}",
+             "\"kernels\": [{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"rot\": %d, \"ms\": %.4f}, "
+             "{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"rot\": %d, \"ms\": %.4f}]}",
              e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, (int)e->fused, e->tune[0].tx, e->tune[0].rows,
-             e->tune[0].depth, e->tune[0].mode, e->tune[0].ms, e->tune[1].tx, e->tune[1].rows,
-             e->tune[1].depth, e->tune[1].mode, e->tune[1].ms);
+             e->tune[0].depth, e->tune[0].mode, e->tune[0].rot, e->tune[0].ms, e->tune[1].tx, e->tune[1].rows,
+             e->tune[1].depth, e->tune[1].mode, e->tune[1].rot, e->tune[1].ms);
     return A3D_OK;
 }
 

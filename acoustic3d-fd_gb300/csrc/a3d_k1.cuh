@@ -52,6 +52,7 @@ struct K1Launch {
     int depth;  // TMA ring depth (0, 1, 2: see Ring in a3d_pipe.cuh; VTI/TTI: 0, 1)
     int mode;   // sweep plan (plan_sweep)
     int rows;   // tile rows per consumer warp (iso: 2 or 4; VTI/TTI: 1)
+    int rot;    // 1: rotated z-tile order of the sweep (Sweep::rot)
 };
 
 cudaError_t launch_k1(const K1Launch &L, cudaStream_t st);

@@ -32,7 +32,7 @@ static cudaError_t k1_launch(Kern kern, int nthreads, size_t smem, long long W, 
 
 // sweep of the updated region [4, nn-4)^3 in 32 x TX tiles; returns gridDim.x
 template <int TX, class Kern>
-static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid, int mode) {
+static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid, int mode, int rot) {
     p.sw.ntz = (p.nnz - 2 * MM + 31) / 32;
     p.sw.ntx = (p.nnx - 2 * MM + TX - 1) / TX;
     p.sw.y_begin = MM;
@@ -45,6 +45,7 @@ static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid,
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nthreads, smem);
     }
     const int g = plan_sweep(p.sw, occ, mode);
+    p.sw.rot = rot ? 1 : 0;
     return grid > 0 ? grid : g;
 }
 

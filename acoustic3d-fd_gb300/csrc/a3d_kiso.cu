@@ -483,7 +483,7 @@ static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
         Maps<5> mp;
         for (int i = 0; i < 5; ++i) mp.m[i] = L.maps[i];
         auto kern = iso_vel<TX, S, D, R>;
-        const int grid = k1_sweep<TX>(p, kern, NT, IsoVelL<TX, S, D>::TOTAL, L.grid, L.mode);
+        const int grid = k1_sweep<TX>(p, kern, NT, IsoVelL<TX, S, D>::TOTAL, L.grid, L.mode, L.rot);
         return k1_launch(kern, NT, IsoVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp,
                          (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
@@ -491,7 +491,7 @@ static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
     Maps<9> mp;
     for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
     auto kern = iso_stress<TX, S, D, R>;
-    const int grid = k1_sweep<TX>(p, kern, NT, IsoStrL<TX, S, D>::TOTAL, L.grid, L.mode);
+    const int grid = k1_sweep<TX>(p, kern, NT, IsoStrL<TX, S, D>::TOTAL, L.grid, L.mode, L.rot);
     return k1_launch(kern, NT, IsoStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, p);
 }
 

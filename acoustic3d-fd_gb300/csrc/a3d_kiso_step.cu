@@ -509,7 +509,7 @@ static cudaError_t launch_step_t(const K1Launch &L, cudaStream_t st) {
     Maps<11> mp;
     for (int i = 0; i < 11; ++i) mp.m[i] = L.maps[i];
     auto kern = iso_step<TX, D, R>;
-    const int grid = k1_sweep<TX>(p, kern, NT, IsoStepL<TX, D>::TOTAL, L.grid, L.mode);
+    const int grid = k1_sweep<TX>(p, kern, NT, IsoStepL<TX, D>::TOTAL, L.grid, L.mode, L.rot);
     return k1_launch(kern, NT, IsoStepL<TX, D>::TOTAL, p.sw.W, grid, st, attr, mp, (float *)L.out0,
                      (float *)L.out1, (float *)L.out2, (float *)L.out3, p);
 }

@@ -543,7 +543,7 @@ static cudaError_t launch_tti_t(const K1Launch &L, cudaStream_t st) {
         Maps<9> mp;
         for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
         auto kern = tti_vel<TX, S, D, R>;
-        const int grid = k1_sweep<TX>(p, kern, NT, TtiVelL<TX, S, D>::TOTAL, L.grid, L.mode);
+        const int grid = k1_sweep<TX>(p, kern, NT, TtiVelL<TX, S, D>::TOTAL, L.grid, L.mode, L.rot);
         return k1_launch(kern, NT, TtiVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0,
                          (S *)L.out1, (S *)L.out2, p);
     }
@@ -551,7 +551,7 @@ static cudaError_t launch_tti_t(const K1Launch &L, cudaStream_t st) {
     Maps<18> mp;
     for (int i = 0; i < 18; ++i) mp.m[i] = L.maps[i];
     auto kern = tti_stress<TX, S, D, R>;
-    const int grid = k1_sweep<TX>(p, kern, NT, TtiStrL<TX, S, D>::TOTAL, L.grid, L.mode);
+    const int grid = k1_sweep<TX>(p, kern, NT, TtiStrL<TX, S, D>::TOTAL, L.grid, L.mode, L.rot);
     return k1_launch(kern, NT, TtiStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, (S *)L.out1, p);
 }
 

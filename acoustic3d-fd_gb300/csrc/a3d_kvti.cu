@@ -519,7 +519,7 @@ static cudaError_t launch_vti_t(const K1Launch &L, cudaStream_t st) {
         Maps<6> mp;
         for (int i = 0; i < 6; ++i) mp.m[i] = L.maps[i];
         auto kern = vti_vel<TX, S, D, R>;
-        const int grid = k1_sweep<TX>(p, kern, NT, VtiVelL<TX, S, D>::TOTAL, L.grid, L.mode);
+        const int grid = k1_sweep<TX>(p, kern, NT, VtiVelL<TX, S, D>::TOTAL, L.grid, L.mode, L.rot);
         return k1_launch(kern, NT, VtiVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0,
                          (S *)L.out1, (S *)L.out2, p);
     }
@@ -527,7 +527,7 @@ static cudaError_t launch_vti_t(const K1Launch &L, cudaStream_t st) {
     Maps<15> mp;
     for (int i = 0; i < 15; ++i) mp.m[i] = L.maps[i];
     auto kern = vti_stress<TX, S, D, R>;
-    const int grid = k1_sweep<TX>(p, kern, NT, VtiStrL<TX, S, D>::TOTAL, L.grid, L.mode);
+    const int grid = k1_sweep<TX>(p, kern, NT, VtiStrL<TX, S, D>::TOTAL, L.grid, L.mode, L.rot);
     return k1_launch(kern, NT, VtiStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, (S *)L.out1, p);
 }
 

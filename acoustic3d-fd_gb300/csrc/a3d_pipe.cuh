@@ -39,8 +39,14 @@ __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long 
     wend = c * full + (long long)(s.tile + 1) * len;
     if (wend > w1) wend = w1;
     s.yb = s.ya + (int)(wend - w);
-    s.z0 = MM + 32 * (s.tile % sw.ntz);
-    s.x0 = MM + TX * (s.tile / sw.ntz);
+    int zt = s.tile % sw.ntz;
+    const int xt = s.tile / sw.ntz;
+    if (sw.rot) {
+        const long long nch = (sw.NY + sw.Yc - 1) / sw.Yc, col = (long long)c * sw.ntx + xt;
+        zt = (int)((zt + col * sw.ntz / (nch * sw.ntx)) % sw.ntz);
+    }
+    s.z0 = MM + 32 * zt;
+    s.x0 = MM + TX * xt;
     s.oa = s.ya;
     s.ob = s.yb;
     s.ya -= EXT;

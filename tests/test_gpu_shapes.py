@@ -1,7 +1,8 @@
 """Every launch configuration the autotuner can pick gives the same record.
 
 The autotuner chooses, per kernel kind and grid, a tile width, rows per lane, ring
-depth and sweep plan; the parity tests see only the configuration it picks on
+depth, sweep plan and (1st-order engines) the z-tile order; the parity tests see
+only the configuration it picks on
 their grids.  Here each configuration is pinned (A3D_TUNE) in turn and its record
 compared bit for bit with the CPU oracle's engine form, on a grid with partial
 tiles in z and x, a y split into several chunks, and PML on every face.
@@ -34,6 +35,8 @@ def _configs(eng):
         for depth in ((0, 1) if eng == "iso_fused" else (0, 1, 2)):
             for plan in (0, 1):
                 out.append(f"{tx},{rows},{depth},{plan}")
+                if eng != "2o":  # the same shape with the rotated z-tile order
+                    out.append(f"{tx},{rows},{depth},{plan},1")
     return out
 
 

@@ -58,7 +58,9 @@ def test_tuned_shapes_are_reused_for_the_same_grid(engine_lib):
     # the second engine ran no candidate launches: its set-up and shot take well under
     # the tuner's dozens of timed launches on this grid
     assert second < 5.0
-    # a pinned shape bypasses the cache and is taken as given
-    os.environ["A3D_TUNE"] = "8,1,0,0;8,1,0,0"
-    _, d3 = _record(a3d, models, tile_x=0)
+    # a pinned shape bypasses the cache and is taken as given, the z-tile order too
+    os.environ["A3D_TUNE"] = "8,1,0,0;8,1,0,0,1"
+    r3, d3 = _record(a3d, models, tile_x=0)
     assert d3["kernels"][0]["tile_x"] == 8 and d3["kernels"][0]["rows"] == 1 and d3["fused"] == 0
+    assert d3["kernels"][0]["rot"] == 0 and d3["kernels"][1]["rot"] == 1
+    assert np.array_equal(r3, r1)
