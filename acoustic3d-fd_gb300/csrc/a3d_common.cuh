@@ -187,10 +187,22 @@ struct Sweep {
     // ntz * (c * ntx + xt) / (chunks * ntx), so CTAs far apart in the sweep (those that
     // share an SM) start from different z tiles
     int rot;
+    // 1 (wave plan, one y chunk): with T tiles and G CTAs, CTA b sweeps the whole
+    // columns of tiles b, b + G, ..., b + (P-1) G (P = T / G), so the CTAs of a wave
+    // hold consecutive tiles and march y in step; the last R = T - P G tiles are cut
+    // into G equal runs of (tile, plane) units, one more run per CTA.  The units of a
+    // CTA form one contiguous range of a virtual order that make_seg decodes.
+    int wave;
 };
 
 __device__ __forceinline__ void cta_range(const Sweep &s, long long &w0, long long &w1) {
     const long long G = gridDim.x, b = blockIdx.x;
+    if (s.wave) {
+        const long long T = (long long)s.ntz * s.ntx, P = T / G, R = T - P * G, NY = s.NY;
+        w0 = b * P * NY + (b * R * NY) / G;
+        w1 = (b + 1) * P * NY + ((b + 1) * R * NY) / G;
+        return;
+    }
     w0 = (s.W * b) / G;
     w1 = (s.W * (b + 1)) / G;
 }

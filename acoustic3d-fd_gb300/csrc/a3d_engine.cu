@@ -46,6 +46,13 @@ int plan_sweep(Sweep &sw, int occ, int mode) {
     const long long slots = (long long)(g_sms > 0 ? g_sms : 148) * (occ > 0 ? occ : 1);
     const long long ntiles = (long long)sw.ntz * sw.ntx;
     sw.W = ntiles * sw.NY;
+    sw.wave = 0;
+    if (mode == 2) {  // wave: whole tile columns in waves of one CTA per slot (Sweep::wave)
+        sw.Yc = sw.NY;
+        sw.wave = 1;
+        const long long g = sw.W / 16 > 1 ? sw.W / 16 : 1;
+        return (int)(slots < g ? slots : g);
+    }
     if (mode == 1) {  // fill: one full wave, chunk length from the nearest chunk count
         long long C = (slots + ntiles / 2) / ntiles;
         const long long cmax = sw.NY / 16 > 1 ? sw.NY / 16 : 1;
@@ -588,7 +595,7 @@ int a3d_engine::autotune_form() {
             int tx = 0, rows = 0, depth = 0, mode = 0, n = 0, rot = 0, n2 = 0;
             if (sscanf(q, "%d,%d,%d,%d%n", &tx, &rows, &depth, &mode, &n) != 4 || (tx != 8 && tx != 16) ||
                 depth < 0 || depth > maxdepth || (fused && rows == 4) ||
-                (rows != 1 && rows != 2 && rows != 4) || (rows == 4 && tx != 16) || mode < 0 || mode > 1)
+                (rows != 1 && rows != 2 && rows != 4) || (rows == 4 && tx != 16) || mode < 0 || mode > 2)
                 return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[,rot][;...], got \"%s\"", env);
             if (q[n] == ',') {
                 if (sscanf(q + n + 1, "%d%n", &rot, &n2) != 1 || rot < 0 || rot > 1)
@@ -611,7 +618,7 @@ int a3d_engine::autotune_form() {
     } else {
         for (auto sh : shapes)
             for (int d = 0; d <= maxdepth; ++d)
-                for (int m = 0; m < 2; ++m)
+                for (int m = 0; m < 3; ++m)
                     if (!fixed_tx || sh.first == fixed_tx) cand.push_back(Tune{sh.first, d, m, sh.second});
     }
     const int kinds = c.physics == A3D_2ORDER || fused ? 1 : 2;

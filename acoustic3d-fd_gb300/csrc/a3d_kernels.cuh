@@ -68,8 +68,9 @@ size_t k2o_smem_bytes(int tx, bool fp64);
 // for occ_per_sm resident CTAs per SM.  Mode 0 (lockstep): if every tile fits
 // in one wave, one CTA per (tile, chunk) with as many chunks as the wave holds
 // (each >= 16 planes), otherwise one wave over whole-y segments.  Mode 1 (fill):
-// one full wave of CTAs, the chunk count rounded to the nearest fit.
-// Fills sw.Yc and sw.W.
+// one full wave of CTAs, the chunk count rounded to the nearest fit.  Mode 2
+// (wave): one wave of CTAs sweeping whole tile columns b, b + G, ... (Sweep::wave).
+// Fills sw.Yc, sw.W and sw.wave.
 int plan_sweep(Sweep &sw, int occ_per_sm, int mode);
 
 // does a CTA with this much dynamic shared memory fit on the current device?

@@ -30,14 +30,34 @@ struct Seg {
 template <int TX, int EXT = 0>
 __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long w1, long long &wend) {
     Seg s;
-    const long long full = (long long)sw.ntz * sw.ntx * sw.Yc;  // units of a full chunk
-    const int c = (int)(w / full);
-    const long long r = w - c * full;
-    const int len = min(sw.Yc, sw.NY - c * sw.Yc);
-    s.tile = (int)(r / len);
-    s.ya = sw.y_begin + c * sw.Yc + (int)(r % len);
-    wend = c * full + (long long)(s.tile + 1) * len;
-    if (wend > w1) wend = w1;
+    int c = 0;
+    if (sw.wave) {  // virtual order of the wave plan (Sweep::wave): this CTA's units
+        const long long G = gridDim.x, b = blockIdx.x, NY = sw.NY;
+        const long long T = (long long)sw.ntz * sw.ntx, P = T / G, R = T - P * G;
+        const long long i = w - (b * P * NY + (b * R * NY) / G);
+        long long tile, y;
+        if (i < P * NY) {  // whole columns: tile b + k G
+            tile = (i / NY) * G + b;
+            y = i % NY;
+        } else {           // this CTA's run of the last R tiles' units
+            const long long q = (b * R * NY) / G + (i - P * NY);
+            tile = P * G + q / NY;
+            y = q % NY;
+        }
+        s.tile = (int)tile;
+        s.ya = sw.y_begin + (int)y;
+        wend = w + (NY - y);  // the column ends
+        if (wend > w1) wend = w1;
+    } else {
+        const long long full = (long long)sw.ntz * sw.ntx * sw.Yc;  // units of a full chunk
+        c = (int)(w / full);
+        const long long r = w - c * full;
+        const int len = min(sw.Yc, sw.NY - c * sw.Yc);
+        s.tile = (int)(r / len);
+        s.ya = sw.y_begin + c * sw.Yc + (int)(r % len);
+        wend = c * full + (long long)(s.tile + 1) * len;
+        if (wend > w1) wend = w1;
+    }
     s.yb = s.ya + (int)(wend - w);
     int zt = s.tile % sw.ntz;
     const int xt = s.tile / sw.ntz;

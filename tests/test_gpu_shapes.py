@@ -33,7 +33,7 @@ def _configs(eng):
     out = []
     for tx, rows in SHAPES[eng]:
         for depth in ((0, 1) if eng == "iso_fused" else (0, 1, 2)):
-            for plan in (0, 1):
+            for plan in (0, 1, 2):
                 out.append(f"{tx},{rows},{depth},{plan}")
                 if eng != "2o":  # the same shape with the rotated z-tile order
                     out.append(f"{tx},{rows},{depth},{plan},1")
