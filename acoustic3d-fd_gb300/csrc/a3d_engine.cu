@@ -628,7 +628,7 @@ int a3d_engine::autotune_form() {
     for (int k = 0; k < kinds; ++k) {
         float best = 1e30f;
         // ms per launch of candidate tc (one warm-up, three timed); f < 0: it does not run
-        auto time_cand = [&](const Tune &tc, float &f) -> int {
+        auto time_cand = [&](const Tune &tc, float &f, int reps) -> int {
             f = -1.0f;
             const int ti = tc.tx == 16 ? 1 : 0;
             auto launch_once = [&]() -> cudaError_t {
@@ -682,34 +682,46 @@ int a3d_engine::autotune_form() {
             if (launch_once() != cudaSuccess) { cudaGetLastError(); return A3D_OK; }
             CUDA_TRY(cudaEventRecord(t0, st));
             bool ok = true;
-            for (int r = 0; r < 3 && ok; ++r) ok = launch_once() == cudaSuccess;
+            for (int r = 0; r < reps && ok; ++r) ok = launch_once() == cudaSuccess;
             CUDA_TRY(cudaEventRecord(t1, st));
             CUDA_TRY(cudaEventSynchronize(t1));
             if (!ok) { cudaGetLastError(); return A3D_OK; }
-            float e3 = 0;
-            CUDA_TRY(cudaEventElapsedTime(&e3, t0, t1));
-            f = e3 / 3;
+            float e = 0;
+            CUDA_TRY(cudaEventElapsedTime(&e, t0, t1));
+            f = e / reps;
             return A3D_OK;
         };
+        // first pass: every candidate, three timed launches
+        std::vector<std::pair<float, Tune>> timed;
         for (const Tune &tc : cand) {
             float f = -1.0f;
-            const int rt = time_cand(tc, f);
+            const int rt = time_cand(tc, f, 3);
+            if (rt) return rt;
+            if (f >= 0.0f) timed.push_back({f, tc});
+        }
+        if (timed.empty()) return fail(A3D_E_CUDA, "no launch configuration of kernel kind %d runs", k);
+        // second pass: the four fastest (and, for the 1st-order engines, each with the
+        // rotated z-tile order) with ten timed launches each, since the leading
+        // candidates often lie within a few percent of each other
+        std::sort(timed.begin(), timed.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        std::vector<Tune> fin;
+        for (size_t i = 0; i < timed.size() && i < 4; ++i) {
+            fin.push_back(timed[i].second);
+            if (c.physics != A3D_2ORDER && !fp64) {
+                Tune r = timed[i].second;
+                r.rot = 1;
+                fin.push_back(r);
+            }
+        }
+        tune[k] = timed[0].second;
+        tune[k].ms = timed[0].first;
+        for (const Tune &tc : fin) {
+            float f = -1.0f;
+            const int rt = time_cand(tc, f, 10);
             if (rt) return rt;
             if (f >= 0.0f && f < best) {
                 best = f;
                 tune[k] = tc;
-                tune[k].ms = f;
-            }
-        }
-        if (best >= 1e30f) return fail(A3D_E_CUDA, "no launch configuration of kernel kind %d runs", k);
-        if (c.physics != A3D_2ORDER && !fp64) {  // the chosen shape with the rotated z-tile order
-            Tune r = tune[k];
-            r.rot = 1;
-            float f = -1.0f;
-            const int rt = time_cand(r, f);
-            if (rt) return rt;
-            if (f >= 0.0f && f < tune[k].ms) {
-                tune[k] = r;
                 tune[k].ms = f;
             }
         }
