@@ -1,7 +1,8 @@
 // a3d_pipe.cuh — the y-marching TMA pipeline shared by every stencil kernel.
 //
-// A CTA owns a contiguous range of the sweep's (tile, plane) space (cta_range),
-// split into segments of consecutive output planes [ya, yb) of one 32 x TX tile.
+// A CTA owns a contiguous range of the sweep's (tile, plane) units (cta_range; in
+// chunk, tile, plane order, or the wave plan's order), split by make_seg into
+// segments of consecutive output planes [ya, yb) of one 32 x TX tile.
 // For each segment it streams planes q = ya-4 .. yb+3; item q carries the copy of
 // plane q of the fields whose y-derivative is taken ("A", kept in an 8-plane
 // register window) and, for q >= ya+4, everything else the update at the output
