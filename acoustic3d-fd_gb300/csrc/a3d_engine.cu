@@ -613,7 +613,7 @@ int a3d_engine::autotune_form() {
         tuned = true;
         return A3D_OK;
     }
-    if (c.tile_x < 0 || fp64) {  // fixed defaults (and the FP64 run): 32x8, shallow rings, both plans
+    if (c.tile_x < 0 || fp64) {  // fixed defaults (and the FP64 run): 32x8, shallow rings, lockstep and fill plans
         for (int m = 0; m < 2; ++m) cand.push_back(Tune{8, 0, m, multirow ? 2 : 1});
     } else {
         for (auto sh : shapes)
