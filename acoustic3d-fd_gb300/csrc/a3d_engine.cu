@@ -625,99 +625,110 @@ int a3d_engine::autotune_form() {
     cudaEvent_t t0, t1;
     CUDA_TRY(cudaEventCreate(&t0));
     CUDA_TRY(cudaEventCreate(&t1));
-    for (int k = 0; k < kinds; ++k) {
-        float best = 1e30f;
-        // ms per launch of candidate tc (one warm-up, three timed); f < 0: it does not run
-        auto time_cand = [&](const Tune &tc, float &f, int reps) -> int {
-            f = -1.0f;
-            const int ti = tc.tx == 16 ? 1 : 0;
-            auto launch_once = [&]() -> cudaError_t {
-                if (c.physics == A3D_2ORDER) {
-                    K2OLaunch L{};
-                    L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
-                    L.tm_cur = m2o_cur[ti][0]; L.tm_prev = m2o_prev[ti][1]; L.tm_vv = m2o_vv[ti];
-                    L.ybuf = Y;
-                    K2OParams &p = L.p;
-                    p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
-                    p.nx = c.nx; p.ny = c.ny; p.gz = -1;
-                    p.fz = fz; p.fx = fx; p.fy = fy;
-                    p.dz2 = p.dx2 = p.dy2 = 1.0f;
-                    p.s_x = p.s_y = p.s_z = -100;
-                    p.rec = rec; p.nt = c.nt; p.err = d_err;
-                    return launch_k2o(L, st);
-                }
-                K1Launch L{};
-                K1Params &p = L.p;
-                p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
-                p.nx = c.nx; p.ny = c.ny; p.npml = npml;
-                p.dtx = p.dty = p.dtz = 0.0f;
-                const float *q = pml;
-                p.cx1 = q; p.cx2 = q + g.nnx; p.ax1 = q + 2 * g.nnx; p.ax2 = q + 3 * g.nnx; q += 4 * g.nnx;
-                p.cy1 = q; p.cy2 = q + g.nny; p.ay1 = q + 2 * g.nny; p.ay2 = q + 3 * g.nny; q += 4 * g.nny;
-                p.cz1 = q; p.cz2 = q + g.nnz; p.az1 = q + 2 * g.nnz; p.az2 = q + 3 * g.nnz;
-                p.s_x = p.s_y = p.s_z = -100;
-                p.taper = taper;
-                p.px = px; p.py = py; p.pz = pz; p.qx = qx; p.qy = qy; p.qz = qz;
-                for (int a = 0; a < 3; ++a) { p.ulo[a] = ulo[a]; p.uhi[a] = uhi[a]; }
-                p.rec = rec; p.nt = c.nt; p.err = d_err;
-                const int kv = c.physics == A3D_ISO ? K1_ISO_VEL : (c.physics == A3D_VTI ? K1_VTI_VEL : K1_TTI_VEL);
-                L.kind = kv + k;
-                L.maps = k == 0 ? mvel[ti] : mstr[ti];
-                L.nmaps = k == 0 ? nvel : nstr;
-                L.out0 = k == 0 ? u : P; L.out1 = k == 0 ? v : Q; L.out2 = w;
-                L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
-                L.half = half;
-                L.rot = tc.rot;
-                p.svp = p.spv = p.rec_scale = 1.0f;
-                if (fused) {  // set 0 read, set 1 written
-                    L.kind = K1_ISO_STEP;
-                    L.maps = mstep[ti][0];
-                    L.nmaps = 11;
-                    L.out0 = u2; L.out1 = v2; L.out2 = w2; L.out3 = P2;
-                    return launch_iso_step(L, st);
-                }
-                auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
-                return launch(L, st);
-            };
-            if (launch_once() != cudaSuccess) { cudaGetLastError(); return A3D_OK; }
+    // one launch of kernel kind kk with shape tc on the engine's fields (no source)
+    auto launch_kind = [&](int kk, const Tune &tc) -> cudaError_t {
+        const int ti = tc.tx == 16 ? 1 : 0;
+        if (c.physics == A3D_2ORDER) {
+            K2OLaunch L{};
+            L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
+            L.tm_cur = m2o_cur[ti][0]; L.tm_prev = m2o_prev[ti][1]; L.tm_vv = m2o_vv[ti];
+            L.ybuf = Y;
+            K2OParams &p = L.p;
+            p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
+            p.nx = c.nx; p.ny = c.ny; p.gz = -1;
+            p.fz = fz; p.fx = fx; p.fy = fy;
+            p.dz2 = p.dx2 = p.dy2 = 1.0f;
+            p.s_x = p.s_y = p.s_z = -100;
+            p.rec = rec; p.nt = c.nt; p.err = d_err;
+            return launch_k2o(L, st);
+        }
+        K1Launch L{};
+        K1Params &p = L.p;
+        p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
+        p.nx = c.nx; p.ny = c.ny; p.npml = npml;
+        p.dtx = p.dty = p.dtz = 0.0f;
+        const float *q = pml;
+        p.cx1 = q; p.cx2 = q + g.nnx; p.ax1 = q + 2 * g.nnx; p.ax2 = q + 3 * g.nnx; q += 4 * g.nnx;
+        p.cy1 = q; p.cy2 = q + g.nny; p.ay1 = q + 2 * g.nny; p.ay2 = q + 3 * g.nny; q += 4 * g.nny;
+        p.cz1 = q; p.cz2 = q + g.nnz; p.az1 = q + 2 * g.nnz; p.az2 = q + 3 * g.nnz;
+        p.s_x = p.s_y = p.s_z = -100;
+        p.taper = taper;
+        p.px = px; p.py = py; p.pz = pz; p.qx = qx; p.qy = qy; p.qz = qz;
+        for (int a = 0; a < 3; ++a) { p.ulo[a] = ulo[a]; p.uhi[a] = uhi[a]; }
+        p.rec = rec; p.nt = c.nt; p.err = d_err;
+        const int kv = c.physics == A3D_ISO ? K1_ISO_VEL : (c.physics == A3D_VTI ? K1_VTI_VEL : K1_TTI_VEL);
+        L.kind = kv + kk;
+        L.maps = kk == 0 ? mvel[ti] : mstr[ti];
+        L.nmaps = kk == 0 ? nvel : nstr;
+        L.out0 = kk == 0 ? u : P; L.out1 = kk == 0 ? v : Q; L.out2 = w;
+        L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
+        L.half = half;
+        L.rot = tc.rot;
+        p.svp = p.spv = p.rec_scale = 1.0f;
+        if (fused) {  // set 0 read, set 1 written
+            L.kind = K1_ISO_STEP;
+            L.maps = mstep[ti][0];
+            L.nmaps = 11;
+            L.out0 = u2; L.out1 = v2; L.out2 = w2; L.out3 = P2;
+            return launch_iso_step(L, st);
+        }
+        auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
+        return launch(L, st);
+    };
+    // ms per launch of candidate tc of kind k: a warm-up launch, then reps timed ones,
+    // each after a launch of the other sweep with shape *other when given, so that
+    // the timed launch meets the L2 contents of the time loop; f < 0: it does not run
+    auto time_cand = [&](int k, const Tune &tc, float &f, int reps, const Tune *other) -> int {
+        f = -1.0f;
+        if (launch_kind(k, tc) != cudaSuccess) { cudaGetLastError(); return A3D_OK; }
+        float sum = 0;
+        for (int r = 0; r < reps; ++r) {
+            if (other && launch_kind(1 - k, *other) != cudaSuccess) { cudaGetLastError(); return A3D_OK; }
             CUDA_TRY(cudaEventRecord(t0, st));
-            bool ok = true;
-            for (int r = 0; r < reps && ok; ++r) ok = launch_once() == cudaSuccess;
+            const cudaError_t le = launch_kind(k, tc);
             CUDA_TRY(cudaEventRecord(t1, st));
             CUDA_TRY(cudaEventSynchronize(t1));
-            if (!ok) { cudaGetLastError(); return A3D_OK; }
+            if (le != cudaSuccess) { cudaGetLastError(); return A3D_OK; }
             float e = 0;
             CUDA_TRY(cudaEventElapsedTime(&e, t0, t1));
-            f = e / reps;
-            return A3D_OK;
-        };
-        // first pass: every candidate, three timed launches
-        std::vector<std::pair<float, Tune>> timed;
+            sum += e;
+        }
+        f = sum / reps;
+        return A3D_OK;
+    };
+    // first pass: every candidate of each kind, three timed launches
+    std::vector<std::pair<float, Tune>> timed[2];
+    for (int k = 0; k < kinds; ++k) {
         for (const Tune &tc : cand) {
             float f = -1.0f;
-            const int rt = time_cand(tc, f, 3);
+            const int rt = time_cand(k, tc, f, 3, nullptr);
             if (rt) return rt;
-            if (f >= 0.0f) timed.push_back({f, tc});
+            if (f >= 0.0f) timed[k].push_back({f, tc});
         }
-        if (timed.empty()) return fail(A3D_E_CUDA, "no launch configuration of kernel kind %d runs", k);
-        // second pass: the four fastest (and, for the 1st-order engines, each with the
-        // rotated z-tile order) with ten timed launches each, since the leading
-        // candidates often lie within a few percent of each other
-        std::sort(timed.begin(), timed.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+        if (timed[k].empty()) return fail(A3D_E_CUDA, "no launch configuration of kernel kind %d runs", k);
+        std::sort(timed[k].begin(), timed[k].end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+        tune[k] = timed[k][0].second;
+        tune[k].ms = timed[k][0].first;
+    }
+    // second pass: the four fastest of each kind (and, for the 1st-order engines, each
+    // with the rotated z-tile order) with ten timed launches each, alternating with
+    // the other sweep's current choice as in the time loop: the leading candidates
+    // often lie within a few percent of each other
+    for (int k = 0; k < kinds; ++k) {
         std::vector<Tune> fin;
-        for (size_t i = 0; i < timed.size() && i < 4; ++i) {
-            fin.push_back(timed[i].second);
+        for (size_t i = 0; i < timed[k].size() && i < 4; ++i) {
+            fin.push_back(timed[k][i].second);
             if (c.physics != A3D_2ORDER && !fp64) {
-                Tune r = timed[i].second;
+                Tune r = timed[k][i].second;
                 r.rot = 1;
                 fin.push_back(r);
             }
         }
-        tune[k] = timed[0].second;
-        tune[k].ms = timed[0].first;
+        const Tune other = kinds == 2 ? tune[1 - k] : Tune{};
+        float best = 1e30f;
         for (const Tune &tc : fin) {
             float f = -1.0f;
-            const int rt = time_cand(tc, f, 10);
+            const int rt = time_cand(k, tc, f, 10, kinds == 2 ? &other : nullptr);
             if (rt) return rt;
             if (f >= 0.0f && f < best) {
                 best = f;
