@@ -15,16 +15,13 @@ __device__ __forceinline__ bool range_damped(int a0, int len, int lo, int hi) {
 }
 
 
-// launch helper: sets the smem attribute once, sizes the grid, launches
+// launch helper: sets the smem attribute once per device, launches
 template <class Kern, class... Args>
 static cudaError_t k1_launch(Kern kern, int nthreads, size_t smem, long long W, int grid,
-                             cudaStream_t st, bool &attr_done, Args... args) {
+                             cudaStream_t st, SmemAttr &attr, Args... args) {
     if (!smem_fits(smem)) return cudaErrorInvalidConfiguration;
-    if (!attr_done) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_done = true;
-    }
+    cudaError_t e = ensure_smem_attr(kern, smem, attr);
+    if (e != cudaSuccess) return e;
     (void)W;
     kern<<<grid, nthreads, smem, st>>>(args...);
     return cudaGetLastError();

@@ -222,14 +222,9 @@ static cudaError_t launch_k2o_t(const K2OLaunch &L, cudaStream_t st) {
     using SM = K2OSmem<TX, S, D>;
     auto kern = k2o_step<TX, S, D, R>;
     constexpr int NT = 32 * (TX / (2 * R) + 1);
-    static bool attr_done = false;
+    static SmemAttr attr;
     if (!smem_fits(SM::TOTAL)) return cudaErrorInvalidConfiguration;
-    if (!attr_done) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)SM::TOTAL);
-        if (e != cudaSuccess) return e;
-        attr_done = true;
-    }
+    if (cudaError_t e = ensure_smem_attr(kern, SM::TOTAL, attr); e != cudaSuccess) return e;
     K2OParams p = L.p;
     p.sw.ntz = (p.nnz - 2 * MM + 31) / 32;
     p.sw.ntx = (p.nnx - 2 * MM + TX - 1) / TX;

@@ -3,6 +3,8 @@
 #pragma once
 #include <cudaTypedefs.h>
 
+#include <atomic>
+
 #include "a3d_common.cuh"
 
 namespace a3d {
@@ -82,6 +84,24 @@ inline bool smem_fits(size_t bytes) {
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
         return false;
     return bytes <= (size_t)optin;
+}
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) applies to the device that is
+// current when it is called, so a launcher records it per device: one bit per
+// device ordinal in an atomic word (ordinals >= 64 set it on every launch).
+struct SmemAttr {
+    std::atomic<unsigned long long> done{0};
+};
+template <class Kern>
+inline cudaError_t ensure_smem_attr(Kern kern, size_t bytes, SmemAttr &a) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+    if (bit && (a.done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess && bit) a.done.fetch_or(bit, std::memory_order_acq_rel);
+    return e;
 }
 
 }  // namespace a3d

@@ -479,7 +479,7 @@ static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
     constexpr int NT = 32 * (TX / (2 * R) + 1);
     if (L.kind == K1_ISO_VEL) {
-        static bool attr = false;
+        static SmemAttr attr;
         Maps<5> mp;
         for (int i = 0; i < 5; ++i) mp.m[i] = L.maps[i];
         auto kern = iso_vel<TX, S, D, R>;
@@ -487,7 +487,7 @@ static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
         return k1_launch(kern, NT, IsoVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp,
                          (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
-    static bool attr = false;
+    static SmemAttr attr;
     Maps<9> mp;
     for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
     auto kern = iso_stress<TX, S, D, R>;

@@ -505,7 +505,7 @@ template <int TX, int D, int R>
 static cudaError_t launch_step_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
     constexpr int NT = 32 * (TX / (2 * R) + 1);
-    static bool attr = false;
+    static SmemAttr attr;
     Maps<11> mp;
     for (int i = 0; i < 11; ++i) mp.m[i] = L.maps[i];
     auto kern = iso_step<TX, D, R>;

@@ -539,7 +539,7 @@ static cudaError_t launch_tti_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
     constexpr int NT = 32 * (TX / (2 * R) + 1);
     if (L.kind == K1_TTI_VEL) {
-        static bool attr = false;
+        static SmemAttr attr;
         Maps<9> mp;
         for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
         auto kern = tti_vel<TX, S, D, R>;
@@ -547,7 +547,7 @@ static cudaError_t launch_tti_t(const K1Launch &L, cudaStream_t st) {
         return k1_launch(kern, NT, TtiVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0,
                          (S *)L.out1, (S *)L.out2, p);
     }
-    static bool attr = false;
+    static SmemAttr attr;
     Maps<18> mp;
     for (int i = 0; i < 18; ++i) mp.m[i] = L.maps[i];
     auto kern = tti_stress<TX, S, D, R>;

@@ -515,7 +515,7 @@ static cudaError_t launch_vti_t(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
     constexpr int NT = 32 * (TX / (2 * R) + 1);
     if (L.kind == K1_VTI_VEL) {
-        static bool attr = false;
+        static SmemAttr attr;
         Maps<6> mp;
         for (int i = 0; i < 6; ++i) mp.m[i] = L.maps[i];
         auto kern = vti_vel<TX, S, D, R>;
@@ -523,7 +523,7 @@ static cudaError_t launch_vti_t(const K1Launch &L, cudaStream_t st) {
         return k1_launch(kern, NT, VtiVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0,
                          (S *)L.out1, (S *)L.out2, p);
     }
-    static bool attr = false;
+    static SmemAttr attr;
     Maps<15> mp;
     for (int i = 0; i < 15; ++i) mp.m[i] = L.maps[i];
     auto kern = vti_stress<TX, S, D, R>;

@@ -20,8 +20,14 @@ A "step" is one shot: the full nt-step time loop over the padded grid.
   rel_l2_vs_fp64  shot-record error of the FP32 run against the same shot run in
          FP64 (GPU FP64 path), outside the timed region
 
---impl reference runs the reference's update restated on the CPU (the reference
-itself is CUDA-only; oracle/time_reference.py times its kernels on the GPU).
+--impl reference times the reference's own implementation of the path, which is
+CUDA: its four .cu files built unchanged for sm_103a into cubins (oracle/_ref, by
+oracle/build_ref.sh where the reference sources are) and driven by
+oracle/_build/refharness, which replays the reference's host loop with its launch
+shapes and its device synchronisations; a bench step is one full shot (or, where a
+shot of the reference takes longer than REF_SAMPLE_S, the first steps of it).
+Where the cubins are absent it times the reference's update restated on the CPU
+(the oracle's literal form, all host cores) instead, and says so.
 Multi-GPU: replicas (torchrun; each rank runs its own shots, no collective in the
 data path); value = all ranks' updates / max rank time.
 """
@@ -230,9 +236,84 @@ def dist_env():
     return ws, rank, local
 
 
+def bench_config(meta, cfgd, ws):
+    """The line's `config`, identical in both arms: the workload description, the
+    replica count and the L2 statement."""
+    eng = cfgd["physics"]
+    pad = cfgd["npml"] + (4 if eng == "2o" else 0)
+    padded = (cfgd["nx"] + 2 * pad) * (cfgd["ny"] + 2 * pad) * ((cfgd["nz"] + 2 * pad + 7) // 8 * 8)
+    nvol = {"2o": 3, "iso": 7, "vti": 11, "tti": 14}[eng]
+    return dict(meta, parallelism=f"replicas{ws}",
+                l2="inputs larger than L2: %d MB of wavefields and model" % (4 * padded * nvol // 2**20))
+
+
+REF_SAMPLE_S = 8.0  # longest reference time loop one bench step of the reference arm runs
+REF_HARNESS = os.path.join(ROOT, "oracle", "_build", "refharness")
+REF_CUBINS = os.path.join(ROOT, "oracle", "_ref")
+REF_CUBIN = {"2o": "ref_2order.cubin", "iso": "ref_1order.cubin", "vti": "ref_vti.cubin", "tti": "ref_tti.cubin"}
+
+
+def reference_cuda_available(eng):
+    return os.path.exists(REF_HARNESS) and os.path.exists(os.path.join(REF_CUBINS, REF_CUBIN[eng]))
+
+
+def run_reference_cuda(args, cfgd, models, shot, meta):
+    """The reference's own CUDA kernels on this GPU: one harness run per bench step,
+    loop time by CUDA events inside the harness, clocks sampled around the timed runs."""
+    import tempfile
+    eng = cfgd["physics"]
+    cells = updated_cells(cfgd)
+    nt = cfgd["nt"]
+    with tempfile.TemporaryDirectory() as d:
+        with open(os.path.join(d, "case.txt"), "w") as f:
+            f.write(f"engine {eng}\nnx {cfgd['nx']}\nny {cfgd['ny']}\nnz {cfgd['nz']}\n")
+            f.write(f"dx {cfgd['dx']}\ndy {cfgd['dy']}\ndz {cfgd['dz']}\n")
+            f.write(f"sx {shot[0]}\nsy {shot[1]}\nsz {shot[2]}\nnt {nt}\n")
+            f.write(f"dt {cfgd['dt']!r}\nfm {cfgd['fm']}\nwtype 1\nmute 0\nsync 1\n")
+        for k, a in models.items():
+            np.ascontiguousarray(a, np.float32).tofile(os.path.join(d, f"{k}.bin"))
+
+        def once(steps):
+            r = subprocess.run([REF_HARNESS, REF_CUBINS, d, str(steps)], capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"refharness failed ({r.returncode}): {r.stderr.strip()[-300:]}")
+            return float(r.stdout.split("ms=")[1].split()[0])
+
+        probe = max(1, min(nt, 50))
+        per = once(probe) / probe  # ms per time step, with the reference's syncs
+        steps = nt if per * nt <= REF_SAMPLE_S * 1000.0 else max(50, int(REF_SAMPLE_S * 1000.0 / per))
+        for _ in range(args.warmup):
+            once(steps)
+        total = 0.0
+        with ClockSampler(0) as clk:
+            for _ in range(args.steps):
+                total += once(steps)
+    value = cells * steps * args.steps / (total / 1000.0) / 1e9
+    return value, total, steps, clk.summary()
+
+
 def run_reference(args, cfgd, models, shot, meta):
     ws, rank, _ = dist_env()
     if rank != 0:
+        return
+    config = bench_config(meta, cfgd, ws)
+    eng = cfgd["physics"]
+    if reference_cuda_available(eng):
+        value, total_ms, steps, clocks = run_reference_cuda(args, cfgd, models, shot, meta)
+        sample = (f"the reference's own CUDA kernels ({REF_CUBIN[eng]}: its .cu built unchanged for sm_103a) "
+                  f"driven by its host loop restated in oracle/refharness.cpp, the reference's launch shapes "
+                  f"and device synchronisations, {steps} of {cfgd['nt']} time steps per bench step, loop time "
+                  f"by CUDA events, on this GPU")
+        line = {"metric": "Gpts/s", "value": value, "unit": "Gpts/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / max(args.steps, 1),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config, "impl": "reference",
+                "reference_kind": "cuda",
+                "cpu_baseline": {"value": value, "unit": "Gpts/s", "cores": 1, "kind": "reference",
+                                 "sample": sample},
+                "e2e": {"value": value, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "clocks": clocks, "gpu_launches": 0}
+        print(json.dumps(line), flush=True)
         return
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -251,7 +332,8 @@ def run_reference(args, cfgd, models, shot, meta):
     line = {"metric": "Gpts/s", "value": value, "unit": "Gpts/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": meta, "impl": "reference",
+            "data": "synthetic", "config": config, "impl": "reference",
+            "reference_kind": "cpu port (reference kernels not built here)",
             "cpu_baseline": {"value": value, "unit": "Gpts/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -462,7 +544,6 @@ def main():
              ("vti", 1): "vti_stress", ("tti", 0): "tti_vel", ("tti", 1): "tti_stress"}.get((eng, dom), "?")
     if desc.get("fused"):
         kname = "iso_step"
-    meta["fused_step"] = bool(desc.get("fused"))
     tr = traffic_per_launch(meta["workload"] + ("" if args.storage == "fp32" else "_" + args.storage))
     traffic = tr.get(kname) if isinstance(tr, dict) else None
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -496,8 +577,6 @@ def main():
     # 2O v; ISO v, rho; VTI v, rho, epsilon, delta; TTI v, epsilon, delta and the host's
     # cos / sin of tilt and azimuth
     n_upload = {"2o": 1, "iso": 2, "vti": 4, "tti": 7}[eng]
-    pad = cfgd["npml"] + (4 if eng == "2o" else 0)
-    padded = (cfgd["nx"] + 2 * pad) * (cfgd["ny"] + 2 * pad) * ((cfgd["nz"] + 2 * pad + 7) // 8 * 8)
     h2d = 4 * cfgd["nx"] * cfgd["ny"] * cfgd["nz"] * n_upload
     d2h = 4 * cfgd["nx"] * cfgd["ny"] * cfgd["nt"]
     e2e_val = None
@@ -525,16 +604,15 @@ def main():
         line = {"metric": "Gpts/s", "value": value, "unit": "Gpts/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": dict(meta, parallelism=f"replicas{ws}",
-                               l2="inputs larger than L2: %d MB of wavefields and model" %
-                                  (4 * padded * (7 if eng == 'iso' else 3) // 2**20),
-                               tile_x=args.tile_x or 8),
+                "config": bench_config(meta, cfgd, ws),
                 "shots_per_hour": 3600.0 * 1000.0 / ms_per_step * ws,
                 "rel_l2_vs_fp64": rel,
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": "Gpts/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "call": "a3d_forward_host"},
-                "wall_s_timed": wall, "clocks": clocks, "tuning": tuning,
+                "wall_s_timed": wall, "clocks": clocks,
+                "tuning": {"fused_step": bool(desc.get("fused")), "tile_x_request": args.tile_x,
+                           "kernels": tuning},
                 "gpu_launches": int(kn[0] + kn[1])}
         print(json.dumps(line), flush=True)
     if group:

@@ -279,7 +279,9 @@ int a3d_closure_teacher(const a3d_closure *c, int sample, float *x_host, float *
  * (three per-axis sponge-factor tables and an error word) lives in one fixed
  * array of A3D_NOALLOC_SCRATCH_BYTES (about 97 KB) that every GPU which loads the
  * library holds until the process exits.  Padded axes above A3D_NOALLOC_MAX_AXIS
- * cells are rejected with A3D_E_ARG.
+ * cells, and padded grids above 2^31 - 1 cells (ldz * nnx * nny; the step indexes
+ * a field with 32-bit offsets, as the engine does), are rejected with A3D_E_ARG
+ * before any GPU work.
  *
  * Buffers (device, float, 16-byte aligned): the padded grid has nnz = nz + 8 +
  * 2*npd cells along z (likewise x, y) and element (iz, ix, iy) at
@@ -290,11 +292,15 @@ int a3d_closure_teacher(const a3d_closure *c, int sample, float *x_host, float *
  * with the next step's dipole amplitude w_next already added, so the two buffers
  * swap roles every step.  `vv` is (v dt)^2 edge-padded.  `rec` ([ny][nx][nt]
  * floats, receivers at model depth rec_z) receives sample `it`, or is NULL.
- * The computation is the engine's 2nd-order step, bit for bit.
+ * The computation is the engine's 2nd-order step with the direct-wave mute off,
+ * bit for bit; the step applies no mute, so callers that want one zero the early
+ * samples of `rec` themselves.
  *
- * The first call on a device sets up the scratch address for that device; make
- * it before any stream capture.  Every call runs on the legacy default stream and
- * waits for the step to finish.  All calls share the scratch array (tables
+ * The first call on a device sets up the scratch address for that device (it is
+ * looked up again after the device's context is re-created, e.g. by
+ * cudaDeviceReset); make that first call before any stream capture.  Every call
+ * runs on the legacy default stream, waits for the step to finish, and leaves the
+ * caller's current device as it found it.  All calls share the scratch array (tables
  * recomputed and error word cleared on each call), so calls that overlap on the
  * GPU — from several host threads, say — race. */
 #define A3D_NOALLOC_MAX_AXIS 4096

@@ -8,10 +8,11 @@
 # x86 code here; the GPU machine is aarch64); refharness.cpp restates the host
 # loop instead and launches the reference kernels through the CUDA driver API.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   default: $A3D_REFERENCE, else a checkout named "reference" beside this repository
 set -euo pipefail
-REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-${A3D_REFERENCE:-$HERE/../../reference}}
 OUT="$HERE/_ref"
 NVCC=${NVCC:-nvcc}
 if [ ! -d "$REF/src" ]; then

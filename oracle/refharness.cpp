@@ -3,8 +3,10 @@
 // TEST INFRASTRUCTURE ONLY.  oracle/build_ref.sh compiles the reference's four
 // .cu files (device code only) into oracle/_ref/*.cubin; this program loads those
 // cubins with the CUDA runtime's library API and replays each engine's host loop
-// (the extern "C" drivers of the reference, restated here because the reference's
-// host code cannot be built for the GPU machine's CPU from this container).  Its
+// (the extern "C" drivers of the reference, restated here: host code compiled on
+// the x86 build machine does not run on the aarch64 GPU machine, there is no
+// aarch64 cross compiler on the build machine, and the reference sources are not
+// present on the GPU machine, so only the device code travels, as cubins).  Its
 // outputs are the golden records that pin the CPU oracle, and its timings are the
 // "reference kernels rebuilt for sm_103a" GPU baseline.
 //
@@ -12,6 +14,10 @@
 //   CASE_DIR/case.txt  "key value" lines: engine (2o|iso|vti|tti) nx ny nz dx dy dz
 //                      sx sy sz nt dt fm wtype mute
 //   CASE_DIR/{vel,rho,eps,del,theta,phi}.bin   raw float32 models, z fastest
+//   optional key "sync 0" drops the device synchronisations the reference's host
+//   loops make after their launches (ISO: 5 per step, ..iso..:523-565; VTI: 4,
+//   ..vti..:557-598; TTI and 2O: none); by default they are made, as the reference
+//   makes them, so the loop time is that of the reference's own host loop.
 // Writes CASE_DIR/rec_ref.bin: the full record rec[it + nt*(ix + nx*iy)] (float32),
 // before the direct-wave mute, and, when mute is 1, CASE_DIR/rec_mute.bin after it;
 // prints one line "refharness <engine> ms=<loop time> steps=<n>".
@@ -149,6 +155,8 @@ int main(int argc, char **argv) {
     const float dt = c.f("dt"), fm = c.f("fm");
     const int wtype = c.kv.count("wtype") ? c.i("wtype") : 1;
     const int mute = c.kv.count("mute") ? c.i("mute") : 0;
+    const bool refsync = c.kv.count("sync") ? c.i("sync") != 0 : true;
+    auto sync = [&]() { if (refsync) CK(cudaDeviceSynchronize()); };
     const int steps = argc > 3 ? atoi(argv[3]) : nt;  // timing runs may stop early
     const size_t nm = (size_t)nx * ny * nz;
     const int is = 0, ns = 1, jsx = 1, jsy = 1, jsz = 1;
@@ -254,21 +262,28 @@ int main(int argc, char **argv) {
             if (iso) {
                 launch(ksrc, dim3(1), dim3(1), -pfac, fsx, fsy, zs, nx, ny, nz, nnx, nny, nnz, dt,
                        t, fm, wt, npml, is, dsx, dsy, P, nsx);
+                sync();
                 launch(ksrc, dim3(1), dim3(1), pfac, fsx, fsy, zs + 2, nx, ny, nz, nnx, nny, nnz,
                        dt, t, fm, wt, npml, is, dsx, dsy, P, nsx);
+                sync();
                 launch(kvel, dimg, dimb, nx, ny, nz, nnx, nny, nnz, npml, dt, dx, dy, dz, u0, v0, w0,
                        u1, v1, w1, P, cx1, cx2, cy1, cy2, cz1, cz2, rho);
+                sync();
                 launch(kstr, dimg, dimb, nx, ny, nz, nnx, nny, nnz, dt, dx, dy, dz, u1, v1, w1, P,
                        vp, rho, npml, px1, px0, py1, py0, pz1, pz0, ax1, ax2, ay1, ay2, az1, az2,
                        fsx, dsx, fsy, dsy, zs, is, nsx);
+                sync();
             } else if (vti) {
                 launch(ksrc, dim3(1), dim3(1), pfac, fsx, fsy, zs, nx, ny, nz, nnx, nny, nnz, dt, t,
                        fm, wt, npml, is, dsx, dsy, P, Q, nsx);
+                sync();
                 launch(kvel, dimg, dimb, nx, ny, nz, nnx, nny, nnz, npml, dt, dx, dy, dz, u0, v0, w0,
                        u1, v1, w1, P, Q, cx1, cx2, cy1, cy2, cz1, cz2, rho);
+                sync();
                 launch(kstr, dimg, dimb, nx, ny, nz, nnx, nny, nnz, dt, dx, dy, dz, u1, v1, w1, P, Q,
                        vp, rho, npml, px1, px0, py1, py0, pz1, pz0, qx1, qx0, qy1, qy0, qz1, qz0,
                        ax1, ax2, ay1, ay2, az1, az2, del, eps, fsx, dsx, fsy, dsy, zs, is, nsx, true);
+                sync();
             } else {
                 launch(ksrc, dim3(1), dim3(1), pfac, fsx, fsy, zs, nx, ny, nz, nnx, nny, nnz, dt, t,
                        fm, wt, npml, is, dsx, dsy, P, Q, nsx);
@@ -289,6 +304,7 @@ int main(int argc, char **argv) {
             }
             launch(krec, dim3((nx * ny + 511) / 512), dim3(512), nnx, nny, nnz, nx, ny, nz, npml, it,
                    nt, P, shot);
+            if (!tti) sync();
         }
         CK(cudaEventRecord(e1));
         CK(cudaEventSynchronize(e1));

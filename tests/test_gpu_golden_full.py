@@ -1,0 +1,78 @@
+"""The CUDA engines against the reference's own CUDA kernels at the benchmark sizes.
+
+The golden files (tests/golden/full/*.npz, made by tests/golden/make_golden_full.py
+on a GB300 from the reference's kernels built for sm_103a) hold, for each
+benchmark workload at its full size, the reference's unmuted record on every
+16th / 32nd receiver line in x and y, the masks of the samples its direct-wave
+mute zeroed and kept there, and the L2 norm of every trace of its full record.
+The models are regenerated here from their seeds and checked against the stored
+hash first.
+
+Gate (the FP32 path's parity bar): relative L2 of the engine's unmuted record
+against the reference's on the stored traces, and of the engine's per-trace norms
+against the reference's over all traces, both within TOL; the engine's mute zeroes
+exactly the samples the reference's mute zeroed on the stored traces.
+"""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FULL_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "full")
+FILES = sorted(glob.glob(os.path.join(FULL_DIR, "*.npz")))
+TOL = 1e-5
+
+
+def _trace_norms(rec):
+    return np.stack([np.linalg.norm(rec[i].astype(np.float64), axis=1) for i in range(rec.shape[0])])
+
+
+def _sha(models):
+    import hashlib
+    h = hashlib.sha256()
+    for k in sorted(models):
+        h.update(k.encode())
+        h.update(np.ascontiguousarray(models[k], np.float32).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f)[:-4] for f in FILES])
+def test_engine_matches_reference_full_size(engine_lib, path):
+    import a3d
+    import bench
+    z = np.load(path)
+    case = json.loads(str(z["case"]))
+    cfgd, models, shot, _ = bench.workload(case["workload"])
+    assert _sha(models) == str(z["model_sha256"]), "the workload generator gave different models here"
+    iy, ix = z["iy"], z["ix"]
+    sel = np.ix_(iy, ix)
+    recs = {}
+    for mute in (False, True):
+        cfg = a3d.make_config(cfgd["physics"], cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"],
+                              dz=cfgd["dz"], nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
+                              rec_z=cfgd.get("rec_z", -1), mute=mute)
+        e = a3d.Engine(cfg, models)
+        try:
+            rec = e.run(*shot)
+        finally:
+            e.close()
+        if not mute:
+            norms = _trace_norms(rec)
+        recs[mute] = np.ascontiguousarray(rec[sel])
+        del rec
+    g = z["rec"]
+    err = rel_l2(recs[False], g)
+    err_n = rel_l2(norms, z["trace_norm"])
+    assert err <= TOL and err_n <= TOL, f"rel-L2 traces {err:.3e}, trace norms {err_n:.3e} (tolerance {TOL:g})"
+    n = g.size
+    zeroed = np.unpackbits(z["zeroed"])[:n].reshape(g.shape).astype(bool)
+    kept = np.unpackbits(z["kept"])[:n].reshape(g.shape).astype(bool)
+    assert zeroed.any(), "the reference's mute zeroed nothing on the stored traces"
+    assert np.all(recs[True][zeroed] == 0), f"{int(np.count_nonzero(recs[True][zeroed]))} samples not muted"
+    assert np.array_equal(recs[True][kept], recs[False][kept]), "the mute changed samples the reference kept"

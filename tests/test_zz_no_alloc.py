@@ -85,3 +85,10 @@ def test_noalloc_step_rejects_oversize_grid(engine_lib):
     rc = step(16, 16, 16, None, big, 8, 8, 20, 64, 10.0, 10.0, 10.0, 1, 1, 1, 0.0, 1, 0, 10, 0)
     assert rc == a3d.A3D_E_ARG
     assert "limit" in a3d.last_error()
+    # every axis within the limit (1400 + 8 + 40 = 1448 cells), but 1448^3 cells
+    # exceed the 2^31 - 1 cells the step's 32-bit offsets reach; rejected before any
+    # GPU work, so the fake pointers are never touched
+    n, npd = 1400, 20
+    rc = step(16, 16, 16, None, n, n, n, npd, 1448, 10.0, 10.0, 10.0, 1, 1, 1, 0.0, 1, 0, 10, 0)
+    assert rc == a3d.A3D_E_ARG
+    assert "2^31" in a3d.last_error()
