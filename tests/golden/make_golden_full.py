@@ -23,6 +23,9 @@ A full record is 0.07-1.5 GB, so each <name>.npz keeps:
   model_sha256  of the model arrays the workload generator produced (the tests
              regenerate the models and check this first)
   ref_loop_ms   the harness's CUDA-event time of the reference's time loop
+  ref_vs_fp64   (with --fp64) relative L2 of the reference's full unmuted record
+             against the same shot run by this build's FP64 engine: how far the
+             reference's own FP32 arithmetic lies from the FP64 solution
 """
 from __future__ import annotations
 
@@ -101,12 +104,30 @@ def trace_norms(rec):
         np.float32)
 
 
+def fp64_distance(cfgd, models, shot, rec):
+    """relative L2 of rec against the same shot run by the FP64 engine"""
+    sys.path.insert(0, os.path.join(ROOT, "acoustic3d-fd_gb300"))
+    import a3d
+    cfg = a3d.make_config(cfgd["physics"], cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"],
+                          dz=cfgd["dz"], nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
+                          rec_z=cfgd.get("rec_z", -1), storage=a3d.FP64)
+    e = a3d.Engine(cfg, models)
+    try:
+        r64 = e.run(*shot)
+    finally:
+        e.close()
+    num = sum(float(np.sum((rec[i].astype(np.float64) - r64[i]) ** 2)) for i in range(rec.shape[0]))
+    den = sum(float(np.sum(r64[i].astype(np.float64) ** 2)) for i in range(rec.shape[0]))
+    return (num / den) ** 0.5
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.join(HERE, "full"))
     ap.add_argument("--harness", default=os.path.join(ROOT, "oracle", "_build", "refharness"))
     ap.add_argument("--cubins", default=os.path.join(ROOT, "oracle", "_ref"))
     ap.add_argument("--only", nargs="*", default=list(WORKLOADS))
+    ap.add_argument("--fp64", action="store_true", help="also store the reference's distance from an FP64 run")
     args = ap.parse_args()
     import bench
     os.makedirs(args.out, exist_ok=True)
@@ -115,7 +136,10 @@ def main():
         cfgd, models, shot, meta = bench.workload(name)
         rec, recm, ms = run_harness(cfgd, models, shot, args.harness, args.cubins)
         s = summarise(rec, recm, shot, cfgd["nx"], cfgd["ny"])
+        del recm
         case = dict(workload=name, **cfgd, shot=list(shot), meta=meta, ref_loop_ms=ms)
+        if args.fp64:
+            s["ref_vs_fp64"] = np.float64(fp64_distance(cfgd, models, shot, rec))
         np.savez_compressed(os.path.join(args.out, name + ".npz"), case=json.dumps(case),
                             model_sha256=model_sha256(models), **s)
         print(f"{name}: reference loop {ms:.1f} ms, max|rec| {float(np.abs(rec).max()):.4g}, "

@@ -10,8 +10,15 @@ hash first.
 
 Gate (the FP32 path's parity bar): relative L2 of the engine's unmuted record
 against the reference's on the stored traces, and of the engine's per-trace norms
-against the reference's over all traces, both within TOL; the engine's mute zeroes
-exactly the samples the reference's mute zeroed on the stored traces.
+against the reference's over all traces, both within TOL = 1e-5; the engine's mute
+zeroes exactly the samples the reference's mute zeroed on the stored traces.
+
+One workload is conditioned worse than that gate: the TTI shot (256^3, 3000 steps,
+azimuth 0-360 deg), whose rotated update amplifies rounding noise, so that the
+reference's own FP32 record lies 2.3e-5 from the same shot run in FP64
+(`ref_vs_fp64` in its golden file).  No FP32 implementation with another operation
+order can then be closer than about that to the reference; there the bound is
+REF_COND x the reference's own distance from the FP64 solution.
 """
 import glob
 import json
@@ -27,6 +34,7 @@ pytestmark = pytest.mark.gpu
 FULL_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "full")
 FILES = sorted(glob.glob(os.path.join(FULL_DIR, "*.npz")))
 TOL = 1e-5
+REF_COND = 1.5
 
 
 def _trace_norms(rec):
@@ -69,7 +77,11 @@ def test_engine_matches_reference_full_size(engine_lib, path):
     g = z["rec"]
     err = rel_l2(recs[False], g)
     err_n = rel_l2(norms, z["trace_norm"])
-    assert err <= TOL and err_n <= TOL, f"rel-L2 traces {err:.3e}, trace norms {err_n:.3e} (tolerance {TOL:g})"
+    tol = TOL
+    if "ref_vs_fp64" in z.files and float(z["ref_vs_fp64"]) > TOL:
+        tol = REF_COND * float(z["ref_vs_fp64"])
+    print(f"{case['workload']}: rel-L2 traces {err:.3e}, trace norms {err_n:.3e}, tolerance {tol:.3g}")
+    assert err <= tol and err_n <= tol, f"rel-L2 traces {err:.3e}, trace norms {err_n:.3e} (tolerance {tol:g})"
     n = g.size
     zeroed = np.unpackbits(z["zeroed"])[:n].reshape(g.shape).astype(bool)
     kept = np.unpackbits(z["kept"])[:n].reshape(g.shape).astype(bool)
