@@ -19,6 +19,12 @@ void clear_error();
 // (a3d_stage.cu); waits for the copy (stream st) and returns an A3D_* code
 int stage_to_device(void *dst, const void *src, size_t bytes, cudaStream_t st);
 
+// copy of a device buffer to the host through the same pinned ring, handing each
+// chunk (host pointer, byte offset, bytes) to sink while the next chunk is copied;
+// returns the first non-zero sink result or an A3D_* code
+int stage_from_device(const void *src, size_t bytes, cudaStream_t st,
+                      const std::function<int(const unsigned char *, size_t, size_t)> &sink);
+
 // tensor map over a padded field (dims nnz, nnx, nny; rows of g.ldz elements)
 // dtype: 0 float, 1 bfloat16, 2 float16, 3 double
 int make_field_map(CUtensorMap *m, const void *base, int dtype, const Grid &g, int box0, int box1);

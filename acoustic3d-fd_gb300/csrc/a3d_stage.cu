@@ -7,11 +7,16 @@
 // kept for the life of the process: host threads copy one chunk of the caller's
 // buffer into a slot while the copy engine moves the previous chunk, so both run
 // at once.  Calls take a process-wide lock (one upload at a time uses the ring);
-// if the ring cannot be allocated, the plain copy runs.  Record downloads stay
-// plain copies: through the ring they were no faster (17-32 GB/s against 26-28),
-// the caller's fresh destination pages being what limits them.
+// if the ring cannot be allocated, the plain copy runs.  Record downloads into a
+// caller's array stay plain copies: through the ring they were no faster (17-32
+// GB/s against 26-28), the caller's fresh destination pages being what limits
+// them.  Downloads that end in a file (the legacy entry points' shot records) go
+// through the ring instead (stage_from_device): the copy engine fills one slot
+// while host threads write the previous one to the file, so the file never waits
+// for a whole-record copy and no pageable copy of the record is made.
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -105,6 +110,52 @@ int stage_to_device(void *dst, const void *src, size_t bytes, cudaStream_t st) {
         if (r == cudaSuccess) r = r2;
     }
     if (r != cudaSuccess) return fail(A3D_E_CUDA, "host-to-device copy of %zu bytes failed: %s", bytes, cudaGetErrorString(r));
+    return A3D_OK;
+}
+
+int stage_from_device(const void *src, size_t bytes, cudaStream_t st,
+                      const std::function<int(const unsigned char *, size_t, size_t)> &sink) {
+    std::lock_guard<std::mutex> lk(g_stage_mu);
+    unsigned char *ring = stage_ring();
+    const unsigned char *s = static_cast<const unsigned char *>(src);
+    const size_t nchunks = (bytes + STAGE_CHUNK - 1) / STAGE_CHUNK;
+    cudaError_t r = cudaSuccess;
+    if (!ring) {  // no pinned ring: plain copies, one chunk at a time
+        std::vector<unsigned char> buf(std::min(bytes, STAGE_CHUNK));
+        for (size_t k = 0; k < nchunks; ++k) {
+            const size_t off = k * STAGE_CHUNK, n = std::min(STAGE_CHUNK, bytes - off);
+            if ((r = cudaMemcpyAsync(buf.data(), s + off, n, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                (r = cudaStreamSynchronize(st)) != cudaSuccess)
+                break;
+            const int rc = sink(buf.data(), off, n);
+            if (rc) return rc;
+        }
+    } else {
+        Events ev;
+        r = ev.make();
+        auto issue = [&](size_t k) -> cudaError_t {
+            const int slot = (int)(k % STAGE_SLOTS);
+            const size_t off = k * STAGE_CHUNK, n = std::min(STAGE_CHUNK, bytes - off);
+            cudaError_t e = cudaMemcpyAsync(ring + slot * STAGE_CHUNK, s + off, n, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaEventRecord(ev.ev[slot], st);
+            return e;
+        };
+        // keep STAGE_SLOTS - 1 copies ahead of the sink; chunk k + SLOTS - 1 reuses the
+        // slot of chunk k - 1, which the sink finished with in the previous iteration
+        for (size_t k = 0; k + 1 < (size_t)STAGE_SLOTS && k < nchunks && r == cudaSuccess; ++k) r = issue(k);
+        int rc = A3D_OK;
+        for (size_t k = 0; k < nchunks && r == cudaSuccess && !rc; ++k) {
+            if (k + STAGE_SLOTS - 1 < nchunks && (r = issue(k + STAGE_SLOTS - 1)) != cudaSuccess) break;
+            const int slot = (int)(k % STAGE_SLOTS);
+            if ((r = cudaEventSynchronize(ev.ev[slot])) != cudaSuccess) break;
+            const size_t off = k * STAGE_CHUNK;
+            rc = sink(ring + slot * STAGE_CHUNK, off, std::min(STAGE_CHUNK, bytes - off));
+        }
+        const cudaError_t r2 = cudaStreamSynchronize(st);  // no slot is in use on return
+        if (r == cudaSuccess) r = r2;
+        if (rc) return rc;
+    }
+    if (r != cudaSuccess) return fail(A3D_E_CUDA, "device-to-host copy of %zu bytes failed: %s", bytes, cudaGetErrorString(r));
     return A3D_OK;
 }
 

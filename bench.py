@@ -100,6 +100,22 @@ def workload(name, nt_override=None):
         return cfg, {"vel": vel}, (64, 64, 5), \
             dict(workload="2order_128cube_3layer_nt%d" % nt, model="128x128x128", dx_m=dx, nt=nt, dt_s=5e-4,
                  sponge=50, fm_hz=25.0, shot=[64, 64, 5], storage="fp32")
+    if name == "2o128lit":
+        # the same model and shot as 2o128 in the configuration's literal form: a
+        # 20-cell absorber, receivers at model depth 5, the direct-wave mute on and a
+        # snapshot of the model window every 100 steps (the reference compiles in a
+        # 50-cell sponge, records at depth 1, leaves its mute commented out and snaps
+        # every 500 steps, so it cannot run this form)
+        import synthetic as S
+        n, dx = 128, 10.0
+        vel = S.layered_2o(n)["vel"]
+        nt = nt_override or 1000
+        cfg = dict(physics="2o", nx=n, ny=n, nz=n, dx=dx, dy=dx, dz=dx, nt=nt, dt=5e-4, fm=25.0, npml=20,
+                   rec_z=5, mute=True, snap_every=100)
+        return cfg, {"vel": vel}, (64, 64, 5), \
+            dict(workload="2order_128cube_3layer_literal_nt%d" % nt, model="128x128x128", dx_m=dx, nt=nt,
+                 dt_s=5e-4, sponge=20, rec_z=5, mute=True, snap_every=100, fm_hz=25.0, shot=[64, 64, 5],
+                 storage="fp32")
     if name == "vti384":
         # 384 x 384 x 256, d 12.5 m, nt 2500, 20-cell PML (the reference's compiled
         # width), smooth seeded fields: v 1500-4500 (seed 3), Gardner density,
@@ -236,6 +252,59 @@ def dist_env():
     return ws, rank, local
 
 
+def legacy_call(cfgd, paths, shotfile, shot, dev):
+    """One call of the reference-facing drop-in entry point of this physics (model
+    files in, decimation 1, record file out, no snapshots), as readmodel.py makes it."""
+    import ctypes
+    from ctypes import c_bool, c_float, c_int
+    import a3d
+    L = a3d.lib()
+    b = lambda x: ctypes.c_char_p(x.encode())
+    g = [c_int(cfgd["nx"]), c_int(cfgd["ny"]), c_int(cfgd["nz"]), c_float(cfgd["dx"]), c_float(cfgd["dy"]),
+         c_float(cfgd["dz"]), c_int(shot[0]), c_int(shot[1]), c_int(shot[2]), c_int(1), c_int(1), c_int(1),
+         c_float(cfgd["dx"]), c_float(cfgd["dy"]), c_float(cfgd["dt"]), c_int(cfgd["nt"])]
+    tail = [c_bool(False), c_bool(False), c_int(100), c_int(dev)]
+    eng, snap = cfgd["physics"], b(os.path.dirname(shotfile) + "/snap_")
+    if eng == "iso":
+        rc = L.cuda_3dfd_1order(b(paths["vel"]), b(paths["rho"]), snap, b(shotfile), c_int(0), c_int(1), *g,
+                                c_float(cfgd["dt"]), c_int(1), c_float(cfgd["fm"]), *tail)
+    elif eng == "vti":
+        rc = L.cuda_3dfd_vti(b(paths["vel"]), b(paths["rho"]), b(paths["eps"]), b(paths["del"]), snap, b(shotfile),
+                             c_int(0), c_int(1), *g, c_float(cfgd["dt"]), c_float(cfgd["fm"]), *tail)
+    elif eng == "tti":
+        rc = L.cuda_3dfd_tti(b(paths["vel"]), b(paths["vel"]), b(paths["eps"]), b(paths["del"]), b(paths["theta"]),
+                             b(paths["phi"]), snap, b(shotfile), c_int(0), c_int(1), *g, c_float(cfgd["dt"]),
+                             c_float(cfgd["fm"]), *tail)
+    else:
+        rc = L.cuda_3dfd(b(paths["vel"]), snap, b(shotfile), c_int(0), c_int(1), *g, c_int(0),
+                         c_float(cfgd["dt"]), c_float(cfgd["fm"]), *tail)
+    if rc != 0:
+        raise RuntimeError(f"legacy entry point returned {rc}: {a3d.last_error()}")
+
+
+def legacy_e2e(cfgd, models, shot, dev, reps=2):
+    """Gpts/s of the drop-in entry point end to end (files in and out, in a temporary
+    directory), one warm call then `reps` timed ones; None where the workload is not
+    the reference's own configuration."""
+    import tempfile
+    if cfgd.get("snap_every") or cfgd.get("mute"):
+        return None
+    with tempfile.TemporaryDirectory() as d:
+        paths = {}
+        for k, a in models.items():
+            paths[k] = os.path.join(d, k + ".bin")
+            np.ascontiguousarray(a, np.float32).tofile(paths[k])
+        shotfile = os.path.join(d, "shot.bin")
+        legacy_call(cfgd, paths, shotfile, shot, dev)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            legacy_call(cfgd, paths, shotfile, shot, dev)
+        sec = (time.perf_counter() - t0) / reps
+    return {"value": updated_cells(cfgd) * cfgd["nt"] / sec / 1e9, "unit": "Gpts/s", "seconds_per_call": sec,
+            "call": {"iso": "cuda_3dfd_1order", "vti": "cuda_3dfd_vti", "tti": "cuda_3dfd_tti",
+                     "2o": "cuda_3dfd"}[cfgd["physics"]] + " (model files in, record file out)"}
+
+
 def bench_config(meta, cfgd, ws):
     """The line's `config`, identical in both arms: the workload description, the
     replica count and the L2 statement."""
@@ -243,8 +312,11 @@ def bench_config(meta, cfgd, ws):
     pad = cfgd["npml"] + (4 if eng == "2o" else 0)
     padded = (cfgd["nx"] + 2 * pad) * (cfgd["ny"] + 2 * pad) * ((cfgd["nz"] + 2 * pad + 7) // 8 * 8)
     nvol = {"2o": 3, "iso": 7, "vti": 11, "tti": 14}[eng]
-    return dict(meta, parallelism=f"replicas{ws}",
-                l2="inputs larger than L2: %d MB of wavefields and model" % (4 * padded * nvol // 2**20))
+    mb = 4 * padded * nvol // 2**20
+    l2 = ("inputs larger than L2: %d MB of wavefields and model" % mb if mb > 126 else
+          "working set %d MB fits the 126 MB L2 (L2-resident; a bench step is a whole shot, whose time "
+          "steps reuse it, so no flush)" % mb)
+    return dict(meta, parallelism=f"replicas{ws}", l2=l2)
 
 
 REF_SAMPLE_S = 8.0  # longest reference time loop one bench step of the reference arm runs
@@ -451,7 +523,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="iso256",
-                    choices=["iso256", "2o128", "vti384", "tti256", "ttiwin", "learned"])
+                    choices=["iso256", "2o128", "2o128lit", "vti384", "tti256", "ttiwin", "learned"])
     ap.add_argument("--params", default="", help="learned: closure weights (.npy; default the package's)")
     ap.add_argument("--windows", type=int, default=4, help="ttiwin: apertures per bench step (of 48)")
     ap.add_argument("--nt", type=int, default=0, help="override nt (profiling runs only)")
@@ -459,6 +531,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error check")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-legacy", action="store_true", help="skip the drop-in entry point's end-to-end timing")
     ap.add_argument("--storage", default="fp32", choices=list(STORAGE),
                     help="wavefield storage (bf16 / fp16: isotropic and VTI engines; arithmetic stays fp32)")
     args = ap.parse_args()
@@ -493,15 +566,24 @@ def main():
     eng = cfgd["physics"]
     cfg = a3d.make_config(eng, cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"],
                           dz=cfgd["dz"], nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
-                          rec_z=cfgd.get("rec_z", -1), tile_x=args.tile_x, storage=STORAGE[args.storage])
+                          rec_z=cfgd.get("rec_z", -1), mute=cfgd.get("mute", False), tile_x=args.tile_x,
+                          storage=STORAGE[args.storage])
     e = a3d.Engine(cfg, models, device=dev)
+    snap_every = cfgd.get("snap_every", 0)
+
+    def shot_device(sx_):
+        """one shot, inputs resident; device ms of its time loop (snapshots, when the
+        workload takes them, cropped on the device and copied out while it runs)"""
+        if snap_every:
+            return e.run(sx_, shot[1], shot[2], snap_every=snap_every, with_time=True)[-1]
+        return e.run_device(sx_, shot[1], shot[2])
     # replicas: the job's shots run along x, one per rank, split round-robin as
     # the reference splits shots over nodes
     import a3d_dist
     job_shots = [(min(cfgd["nx"] - 1, shot[0] + 4 * k), shot[1], shot[2]) for k in range(ws)]
     sx = a3d_dist.shots_for_rank(job_shots, rank, ws)[0][0]
     for _ in range(args.warmup):
-        e.run_device(sx, shot[1], shot[2])
+        shot_device(sx)
 
     def barrier():
         if group:
@@ -511,14 +593,18 @@ def main():
 
     # ---- timed region: K shots, inputs resident
     barrier()
-    e.set_profiling(True)
+    if not snap_every:
+        e.set_profiling(True)
     dev_ms = 0.0
     with ClockSampler(dev) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            dev_ms += e.run_device(sx, shot[1], shot[2])
+            dev_ms += shot_device(sx)
         wall = time.perf_counter() - t0
     barrier()
+    if snap_every:  # kernel events separately, on one shot without snapshots
+        e.set_profiling(True)
+        e.run_device(sx, shot[1], shot[2])
     kms, kn = e.kernel_times()
     e.set_profiling(False)
     desc = e.describe()
@@ -564,7 +650,7 @@ def main():
         rec32 = e.run(sx, shot[1], shot[2])
         cfg64 = a3d.make_config(eng, cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"],
                                 dz=cfgd["dz"], nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
-                                rec_z=cfgd.get("rec_z", -1), storage=a3d.FP64)
+                                rec_z=cfgd.get("rec_z", -1), mute=cfgd.get("mute", False), storage=a3d.FP64)
         e64 = a3d.Engine(cfg64, models, device=dev)
         rec64 = e64.run(sx, shot[1], shot[2])
         e64.close()
@@ -580,15 +666,33 @@ def main():
     h2d = 4 * cfgd["nx"] * cfgd["ny"] * cfgd["nz"] * n_upload
     d2h = 4 * cfgd["nx"] * cfgd["ny"] * cfgd["nt"]
     e2e_val = None
+    if snap_every:  # snapshots come back as host arrays: one window per snapshot
+        d2h += 4 * cfgd["nx"] * cfgd["ny"] * cfgd["nz"] * len(range(0, cfgd["nt"], snap_every))
+
+    def e2e_once():
+        if not snap_every:
+            a3d.forward_host(cfg, models, [(sx, shot[1], shot[2])], device=dev)
+            return
+        eh = a3d.Engine(cfg, models, device=dev)  # model upload and set-up
+        try:
+            eh.run(sx, shot[1], shot[2], snap_every=snap_every)
+        finally:
+            eh.close()
+
     if args.e2e_steps > 0:
-        a3d.forward_host(cfg, models, [(sx, shot[1], shot[2])], device=dev)  # warm
+        e2e_once()  # warm
         barrier()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
-            a3d.forward_host(cfg, models, [(sx, shot[1], shot[2])], device=dev)
+            e2e_once()
         e2e_s = time.perf_counter() - t0
         barrier()
         e2e_val = cells * nt * args.e2e_steps * ws / e2e_s / 1e9
+
+    # ---- the drop-in entry point end to end (model files in, record file out)
+    legacy = None
+    if rank == 0 and args.storage == "fp32" and not args.no_legacy:
+        legacy = legacy_e2e(cfgd, models, (sx, shot[1], shot[2]), dev)
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -609,11 +713,15 @@ def main():
                 "rel_l2_vs_fp64": rel,
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_val, "unit": "Gpts/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                        "call": "a3d_forward_host"},
+                        "call": "a3d_engine_create + a3d_engine_run (record and snapshots to host) + destroy"
+                        if snap_every else "a3d_forward_host", "legacy_entry_point": legacy},
                 "wall_s_timed": wall, "clocks": clocks,
                 "tuning": {"fused_step": bool(desc.get("fused")), "tile_x_request": args.tile_x,
                            "kernels": tuning},
-                "gpu_launches": int(kn[0] + kn[1])}
+                # our kernels in the timed region: the step kernels, plus one crop per
+                # snapshot when the workload takes snapshots
+                "gpu_launches": int(kn[0] + kn[1]) if not snap_every else
+                args.steps * (nt + len(range(0, nt, snap_every)))}
         print(json.dumps(line), flush=True)
     if group:
         group.destroy_process_group()
