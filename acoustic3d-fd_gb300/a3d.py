@@ -33,7 +33,7 @@ class Config(ctypes.Structure):
                 ("nt", ctypes.c_int), ("dt", ctypes.c_float), ("fm", ctypes.c_float),
                 ("wtype", ctypes.c_int), ("npml", ctypes.c_int), ("rec_z", ctypes.c_int),
                 ("mute", ctypes.c_int), ("storage", ctypes.c_int), ("tile_x", ctypes.c_int),
-                ("boundary", ctypes.c_int)]
+                ("boundary", ctypes.c_int), ("batch", ctypes.c_int)]
 
 
 BOUNDARY_PML, BOUNDARY_LEARNED = 0, 1
@@ -89,6 +89,11 @@ def lib() -> ctypes.CDLL:
         L.a3d_engine_run.restype = ctypes.c_int
         L.a3d_engine_run_device.argtypes = [vp, ctypes.POINTER(ShotPos), vp, ctypes.POINTER(ctypes.c_double)]
         L.a3d_engine_run_device.restype = ctypes.c_int
+        L.a3d_engine_run_shots.argtypes = [vp, ctypes.POINTER(ShotPos), ctypes.c_int, _FP,
+                                           ctypes.POINTER(ctypes.c_double)]
+        L.a3d_engine_run_shots.restype = ctypes.c_int
+        L.a3d_engine_copy_record.argtypes = [vp, ctypes.c_int, _FP]
+        L.a3d_engine_copy_record.restype = ctypes.c_int
         L.a3d_engine_record_device.argtypes = [vp]
         L.a3d_engine_record_device.restype = vp
         L.a3d_engine_device_bytes.argtypes = [vp]
@@ -159,13 +164,14 @@ def _fptr(a):
 
 
 def make_config(physics, nx, ny, nz, dx=10.0, dy=10.0, dz=10.0, nt=100, dt=1e-3, fm=20.0, wtype=1,
-                npml=0, rec_z=-1, mute=False, storage=FP32, tile_x=0, boundary=BOUNDARY_PML) -> Config:
+                npml=0, rec_z=-1, mute=False, storage=FP32, tile_x=0, boundary=BOUNDARY_PML, batch=0) -> Config:
+    """batch > 1 (VTI): the engine runs up to `batch` shots per launch (Engine.run_shots)."""
     if isinstance(physics, str):
         physics = PHYSICS[physics]
     if isinstance(boundary, str):
         boundary = BOUNDARIES[boundary]
     return Config(physics, nx, ny, nz, dx, dy, dz, nt, dt, fm, wtype, npml, rec_z, int(mute), storage, tile_x,
-                  boundary)
+                  boundary, batch)
 
 
 class Engine:
@@ -218,6 +224,25 @@ class Engine:
         if with_time:
             out += (ms.value,)
         return out[0] if len(out) == 1 else out
+
+    def run_shots(self, shots, with_time=False, to_host=True):
+        """Multi-shot sweep (engine made with batch >= len(shots)): records
+        [k, ny, nx, nt] (None with to_host=False: they stay on the device), and the
+        device ms of the time loop with with_time."""
+        c = self.cfg
+        k = len(shots)
+        arr = (ShotPos * max(k, 1))(*[ShotPos(*s) for s in shots])
+        recs = np.zeros((k, c.ny, c.nx, c.nt), np.float32) if to_host else None
+        ms = ctypes.c_double(0.0)
+        _check(lib().a3d_engine_run_shots(self.h, arr, k, _fptr(recs), ctypes.byref(ms)))
+        return (recs, ms.value) if with_time else recs
+
+    def record(self, j=0):
+        """The record [ny, nx, nt] of shot j of the last run (a3d_engine_copy_record)."""
+        c = self.cfg
+        rec = np.zeros((c.ny, c.nx, c.nt), np.float32)
+        _check(lib().a3d_engine_copy_record(self.h, j, _fptr(rec)))
+        return rec
 
     def run_device(self, sx, sy, sz, rec_dev_ptr=None) -> float:
         """Run one shot leaving the record on the device; returns device ms."""

@@ -5,7 +5,9 @@
 // model files, allocates, runs, writes and frees).  Here one call keeps an engine
 // (model resident in HBM, tensor maps built, launch shapes tuned) for as long as
 // consecutive shots use the same window, and carries the tuned launch shapes
-// over to the engines of later windows.
+// over to the engines of later windows.  With cfg.batch = K > 1 (VTI) consecutive
+// shots on the same window run K at a time as multi-shot sweeps (one launch per
+// kernel and step for all K), each shot's record the same as its single run.
 #include <cstring>
 #include <functional>
 #include <thread>
@@ -58,7 +60,8 @@ extern "C" int a3d_run_batch(const a3d_problem *pb, const a3d_shot *shots, int n
     bool have_tune = false, fused = false;
     size_t off = 0;
     int rc = A3D_OK;
-    for (int i = 0; i < nshot && rc == A3D_OK; ++i) {
+    const int K = c.batch > 1 ? c.batch : 1;
+    for (int i = 0; i < nshot && rc == A3D_OK;) {
         const a3d_window w = (o->windows && o->windows[i].nx != 0) ? o->windows[i] : whole;
         if (!e || !same_window(w, cur)) {
             if (e) a3d_engine_destroy(e);
@@ -105,9 +108,19 @@ extern "C" int a3d_run_batch(const a3d_problem *pb, const a3d_shot *shots, int n
             cur = w;
         }
         e->graph = o->graph != 0;
-        const a3d_shot rel{shots[i].sx - w.x0, shots[i].sy - w.y0, shots[i].sz - w.z0};
+        // this shot and the following ones on the same window, up to K of them
+        int k = 1;
+        while (k < K && i + k < nshot &&
+               same_window((o->windows && o->windows[i + k].nx != 0) ? o->windows[i + k] : whole, w))
+            ++k;
+        std::vector<a3d_shot> rel(k);
+        for (int j = 0; j < k; ++j)
+            rel[j] = a3d_shot{shots[i + j].sx - w.x0, shots[i + j].sy - w.y0, shots[i + j].sz - w.z0};
         double ms = 0;
-        rc = a3d_engine_run(e, &rel, o->recs_host ? o->recs_host + off : nullptr, 0, 0, nullptr, &ms);
+        if (K > 1)
+            rc = a3d_engine_run_shots(e, rel.data(), k, o->recs_host ? o->recs_host + off : nullptr, &ms);
+        else
+            rc = a3d_engine_run(e, &rel[0], o->recs_host ? o->recs_host + off : nullptr, 0, 0, nullptr, &ms);
         if (rc) break;
         if (!have_tune) {
             tune[0] = e->tune[0];
@@ -115,9 +128,12 @@ extern "C" int a3d_run_batch(const a3d_problem *pb, const a3d_shot *shots, int n
             fused = e->fused;
             have_tune = true;
         }
-        if (o->rec_offsets) o->rec_offsets[i] = off;
-        if (o->ms) o->ms[i] = ms;
-        off += (size_t)c.nt * w.nx * w.ny;
+        for (int j = 0; j < k; ++j) {  // a sweep's device time is shared evenly by its shots
+            if (o->rec_offsets) o->rec_offsets[i + j] = off;
+            if (o->ms) o->ms[i + j] = ms / k;
+            off += (size_t)c.nt * w.nx * w.ny;
+        }
+        i += k;
     }
     if (e) a3d_engine_destroy(e);
     return rc;

@@ -148,6 +148,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
     }
 }
 
+// 4-D tiled TMA load (box {b0,b1,1,1}): a field of several shots, the 4th
+// coordinate selecting the shot
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int c0, int c1, int c2, int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // 3-D tiled TMA load of box {b0,b1,1} at coordinates (c0,c1,c2) into smem,
 // completing on `bar` (CTA-local destination address).
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar,
@@ -172,17 +183,22 @@ __device__ __forceinline__ void consumer_sync(int nthreads) {
 // work split: the (tile, plane) space of a sweep is cut along y into chunks of
 // Yc planes (the last one may be shorter) and linearised chunk-major:
 //     w = c * (ntiles * Yc) + tile * len_c + (y - y_begin - c * Yc),
-//     tile = tz + ntz * tx,  len_c = planes of chunk c,
+//     tile = shot + nshot * (tz + ntz * tx),  len_c = planes of chunk c,
 // then split into gridDim.x contiguous ranges of nearly equal length.  With one
 // chunk-segment per CTA (the host picks Yc so), CTAs that run concurrently march
 // the same y range and neighbouring tiles read each other's halos from L2.
+// A sweep over several shots of one model (nshot > 1) takes the shot as the
+// fastest part of the tile index, so the CTAs that hold one tile of the grid for
+// the different shots run at the same time and read its model parameters once
+// from HBM, the others from L2.
 
 struct Sweep {
     int ntz, ntx;    // tiles along z and x
+    int nshot;       // shots advanced together (>= 1)
     int y_begin;     // first output plane
     int NY;          // output planes per tile
     int Yc;          // planes per y chunk
-    long long W;     // ntz * ntx * NY
+    long long W;     // ntz * ntx * nshot * NY
     // 1: column (chunk c, x tile xt) visits its z tiles rotated by
     // ntz * (c * ntx + xt) / (chunks * ntx), so CTAs far apart in the sweep (those that
     // share an SM) start from different z tiles
@@ -198,7 +214,7 @@ struct Sweep {
 __device__ __forceinline__ void cta_range(const Sweep &s, long long &w0, long long &w1) {
     const long long G = gridDim.x, b = blockIdx.x;
     if (s.wave) {
-        const long long T = (long long)s.ntz * s.ntx, P = T / G, R = T - P * G, NY = s.NY;
+        const long long T = (long long)s.ntz * s.ntx * s.nshot, P = T / G, R = T - P * G, NY = s.NY;
         w0 = b * P * NY + (b * R * NY) / G;
         w1 = (b + 1) * P * NY + ((b + 1) * R * NY) / G;
         return;

@@ -44,7 +44,8 @@ void clear_error() { g_err.clear(); }
 static int g_sms = 0;
 int plan_sweep(Sweep &sw, int occ, int mode) {
     const long long slots = (long long)(g_sms > 0 ? g_sms : 148) * (occ > 0 ? occ : 1);
-    const long long ntiles = (long long)sw.ntz * sw.ntx;
+    if (sw.nshot < 1) sw.nshot = 1;
+    const long long ntiles = (long long)sw.ntz * sw.ntx * sw.nshot;
     sw.W = ntiles * sw.NY;
     sw.wave = 0;
     if (mode == 2) {  // wave: whole tile columns in waves of one CTA per slot (Sweep::wave)
@@ -90,21 +91,25 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 // dtype: 0 float, 1 bfloat16, 2 float16, 3 double.  A 2-byte field's base (the
 // allocation + zoff elements) is only 8-byte aligned, so its map starts 4 elements
 // earlier (16-byte aligned) and kernels add 4 to its z coordinates.
-static int make_map(CUtensorMap *m, const void *base, int dtype, const Grid &g, int box0, int box1) {
+// With nshot > 1 the map is 4-D: nshot copies of the field, shot_bytes apart (the
+// 4th coordinate selects the shot of a multi-shot sweep).
+static int make_map(CUtensorMap *m, const void *base, int dtype, const Grid &g, int box0, int box1,
+                    int nshot = 1, size_t shot_bytes = 0) {
     auto enc = encode_fn();
     if (!enc) return fail(A3D_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
     const size_t es = dtype == 3 ? 8 : (dtype == 0 ? 4 : 2);
     const int zs = es == 2 ? 4 : 0;
     const char *b = static_cast<const char *>(base) - zs * es;
-    cuuint64_t dims[3] = {(cuuint64_t)(g.nnz + zs), (cuuint64_t)g.nnx, (cuuint64_t)g.nny};
-    cuuint64_t strides[2] = {(cuuint64_t)(g.ldz * es), (cuuint64_t)((size_t)g.ldz * g.nnx * es)};
-    cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, 1};
-    cuuint32_t estr[3] = {1, 1, 1};
+    cuuint64_t dims[4] = {(cuuint64_t)(g.nnz + zs), (cuuint64_t)g.nnx, (cuuint64_t)g.nny, (cuuint64_t)nshot};
+    cuuint64_t strides[3] = {(cuuint64_t)(g.ldz * es), (cuuint64_t)((size_t)g.ldz * g.nnx * es),
+                             (cuuint64_t)shot_bytes};
+    cuuint32_t box[4] = {(cuuint32_t)box0, (cuuint32_t)box1, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
     const CUtensorMapDataType dt = dtype == 3   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
                                    : dtype == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
                                    : dtype == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-    CUresult r = enc(m, dt, 3, const_cast<char *>(b), dims, strides, box, estr,
+    CUresult r = enc(m, dt, nshot > 1 ? 4 : 3, const_cast<char *>(b), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                      CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(A3D_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
@@ -168,6 +173,11 @@ void *a3d_engine::dalloc(size_t bytes) {
 void *a3d_engine::dfield(size_t es) {
     char *p = (char *)dalloc(g.elems() * es);
     return p ? p + Grid::zoff * es : nullptr;
+}
+
+void *a3d_engine::dfield_batch() {
+    char *p = (char *)dalloc(fstride * esz * nbatch);
+    return p ? p + Grid::zoff * esz : nullptr;
 }
 
 // edge-replicated padding of a model on the device: the reference's three one-axis
@@ -243,14 +253,20 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     float *raw = nullptr;  // device scratch for one model array
     CUDA_TRY(cudaMalloc(&raw, (size_t)c.nx * c.ny * c.nz * 4));
     struct FreeRaw { float *p; ~FreeRaw() { cudaFree(p); } } free_raw{raw};
-    const size_t fb = g.elems() * e->esz;
+    const size_t fb = e->nbatch > 1 ? e->fstride * e->esz * e->nbatch : g.elems() * e->esz;
     auto field = [&](void **p) -> int {
-        *p = e->dfield(e->esz);
+        *p = e->nbatch > 1 ? e->dfield_batch() : e->dfield(e->esz);
         return *p ? A3D_OK : fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", fb);
     };
     int rc;
-    e->rec = (float *)e->dalloc((size_t)c.nt * c.nx * c.ny * 4);
-    e->d_mute = (int *)e->dalloc((size_t)c.nx * c.ny * 4);
+    e->rec = (float *)e->dalloc((size_t)c.nt * c.nx * c.ny * 4 * e->nbatch);
+    e->d_mute = (int *)e->dalloc((size_t)c.nx * c.ny * 4 * e->nbatch);
+    if (e->nbatch > 1) {  // shot cells far outside the grid until a run sets them
+        std::vector<int4> far(e->nbatch, make_int4(-100, -100, -100, 0));
+        e->d_shots = (int4 *)e->dalloc(far.size() * sizeof(int4));
+        if (!e->d_shots) return fail(A3D_E_NOMEM, "device allocation failed");
+        CUDA_TRY(cudaMemcpy(e->d_shots, far.data(), far.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    }
     e->snap_dev = (float *)e->dalloc((size_t)c.nx * c.ny * c.nz * 4);
     if (!e->rec || !e->d_mute || !e->snap_dev) return fail(A3D_E_NOMEM, "record allocation failed");
 
@@ -410,6 +426,8 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     int b0, b1;
     auto mk = [&](CUtensorMap *m, const void *p, bool isfield, int box) {
         box_dims(box, tx, b0, b1, isfield && e->half ? 48 : 40);
+        if (isfield && e->nbatch > 1)  // every shot's copy of a wavefield: 4-D map
+            return make_map(m, p, f64 ? 3 : e->half, g, b0, b1, e->nbatch, e->fstride * e->esz);
         return make_map(m, p, isfield ? (f64 ? 3 : e->half) : 0, g, b0, b1);
     };
     if (c.physics == A3D_ISO) {
@@ -519,8 +537,8 @@ int a3d_engine::autotune() {
         return autotune_form();
     }
     char key[256];
-    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", device, cfg.physics, cfg.storage, g.nnz, g.nnx, g.nny,
-             npml, (int)learned, (int)fused_ok, cfg.tile_x);
+    snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", device, cfg.physics, cfg.storage, g.nnz, g.nnx,
+             g.nny, npml, (int)learned, (int)fused_ok, cfg.tile_x, nbatch);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);
@@ -664,6 +682,13 @@ int a3d_engine::autotune_form() {
         L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
         L.half = half;
         L.rot = tc.rot;
+        if (nbatch > 1) {  // multi-shot kernels over every copy (no source: d_shots lie outside)
+            L.ms = 1;
+            L.nshot = nbatch;
+            p.shots = d_shots;
+            p.fstride = fstride;
+            p.rstride = (size_t)c.nt * c.nx * c.ny;
+        }
         p.svp = p.spv = p.rec_scale = 1.0f;
         if (fused) {  // set 0 read, set 1 written
             L.kind = K1_ISO_STEP;
@@ -759,8 +784,51 @@ int a3d_engine::snap_setup() {
     return A3D_OK;
 }
 
+// Runs loop() between ev0 and ev1 on the engine stream.  With use_graph it is
+// captured into a CUDA graph first and the graph is launched once, so the steps go
+// to the GPU as one submission.
+static int timed_loop(a3d_engine *e, bool use_graph, const std::function<int()> &loop) {
+    cudaStream_t st = e->st;
+    if (!use_graph) {
+        CUDA_TRY(cudaEventRecord(e->ev0, st));
+        int r = loop();
+        if (r) return r;
+        CUDA_TRY(cudaEventRecord(e->ev1, st));
+        return A3D_OK;
+    }
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    const int r = loop();
+    cudaGraph_t gr = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &gr);
+    if (r || ec != cudaSuccess) {
+        if (gr) cudaGraphDestroy(gr);
+        return r ? r : fail(A3D_E_CUDA, "stream capture of the time loop failed: %s", cudaGetErrorString(ec));
+    }
+    cudaGraphExec_t ge = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&ge, gr, 0);
+    cudaGraphDestroy(gr);
+    if (ei != cudaSuccess) return fail(A3D_E_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(ei));
+    cudaError_t el = cudaEventRecord(e->ev0, st);
+    if (el == cudaSuccess) el = cudaGraphLaunch(ge, st);
+    if (el == cudaSuccess) el = cudaEventRecord(e->ev1, st);
+    if (el == cudaSuccess) el = cudaStreamSynchronize(st);
+    cudaGraphExecDestroy(ge);
+    if (el != cudaSuccess) return fail(A3D_E_CUDA, "graph launch of the time loop failed: %s", cudaGetErrorString(el));
+    return A3D_OK;
+}
+
 int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, double *ms) {
     const a3d_config &c = cfg;
+    if (nbatch > 1) {  // an engine of multi-shot sweeps runs a single shot as a sweep of one
+        if (hook && hook->want) return fail(A3D_E_UNSUPPORTED, "snapshots are not taken in multi-shot sweeps");
+        int r = run_shots(&s, 1, ms);
+        if (!r && rec_dev && rec_dev != rec) {
+            cudaError_t ce = cudaMemcpyAsync(rec_dev, rec, (size_t)c.nt * c.nx * c.ny * 4, cudaMemcpyDeviceToDevice, st);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+            if (ce != cudaSuccess) r = fail(A3D_E_CUDA, "record copy failed: %s", cudaGetErrorString(ce));
+        }
+        return r;
+    }
     if (s.sx < 0 || s.sx >= c.nx || s.sy < 0 || s.sy >= c.ny || s.sz < 0 || s.sz >= c.nz)
         return fail(A3D_E_ARG, "shot (%d,%d,%d) outside the %dx%dx%d model", s.sx, s.sy, s.sz, c.nx, c.ny, c.nz);
     if (!rec_dev) rec_dev = rec;
@@ -825,38 +893,10 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         ++nsnap;
         return A3D_OK;
     };
-    // the time loop, bracketed by ev0/ev1; with graph mode (and no snapshot or
-    // per-kernel events in the loop) it is captured into a CUDA graph first and the
-    // graph is launched once, so the steps go to the GPU as one submission
+    // the time loop, bracketed by ev0/ev1 (graph replay when graph mode is on and no
+    // snapshot or per-kernel events sit in the loop)
     const bool use_graph = graph && !profiling && !(hook && hook->want);
-    auto time_loop = [&](auto &&loop) -> int {
-        if (!use_graph) {
-            CUDA_TRY(cudaEventRecord(ev0, st));
-            int r = loop();
-            if (r) return r;
-            CUDA_TRY(cudaEventRecord(ev1, st));
-            return A3D_OK;
-        }
-        CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-        const int r = loop();
-        cudaGraph_t gr = nullptr;
-        const cudaError_t ec = cudaStreamEndCapture(st, &gr);
-        if (r || ec != cudaSuccess) {
-            if (gr) cudaGraphDestroy(gr);
-            return r ? r : fail(A3D_E_CUDA, "stream capture of the time loop failed: %s", cudaGetErrorString(ec));
-        }
-        cudaGraphExec_t ge = nullptr;
-        const cudaError_t ei = cudaGraphInstantiate(&ge, gr, 0);
-        cudaGraphDestroy(gr);
-        if (ei != cudaSuccess) return fail(A3D_E_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(ei));
-        cudaError_t el = cudaEventRecord(ev0, st);
-        if (el == cudaSuccess) el = cudaGraphLaunch(ge, st);
-        if (el == cudaSuccess) el = cudaEventRecord(ev1, st);
-        if (el == cudaSuccess) el = cudaStreamSynchronize(st);
-        cudaGraphExecDestroy(ge);
-        if (el != cudaSuccess) return fail(A3D_E_CUDA, "graph launch of the time loop failed: %s", cudaGetErrorString(el));
-        return A3D_OK;
-    };
+    auto time_loop = [&](auto &&loop) -> int { return timed_loop(this, use_graph, loop); };
     if (c.physics == A3D_2ORDER) {
         CUDA_TRY(cudaMemsetAsync(field_alloc(X, esz), 0, fb, st));
         CUDA_TRY(cudaMemsetAsync(field_alloc(Y, esz), 0, fb, st));
@@ -1044,6 +1084,112 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
     return A3D_OK;
 }
 
+// Multi-shot sweeps: k shots of this model advance together, every launch covering
+// all of them (their wavefields lie fstride elements apart; their records and mute
+// tables follow each other).  The arithmetic of each shot is that of run(), so each
+// record equals its one-shot run bit for bit.
+int a3d_engine::run_shots(const a3d_shot *shots, int k, double *ms) {
+    const a3d_config &c = cfg;
+    if (nbatch <= 1) return fail(A3D_E_ARG, "the engine was created without multi-shot sweeps (cfg.batch <= 1)");
+    if (!shots || k < 1 || k > nbatch) return fail(A3D_E_ARG, "%d shots for an engine of %d", k, nbatch);
+    for (int j = 0; j < k; ++j) {
+        const a3d_shot &s = shots[j];
+        if (s.sx < 0 || s.sx >= c.nx || s.sy < 0 || s.sy >= c.ny || s.sz < 0 || s.sz >= c.nz)
+            return fail(A3D_E_ARG, "shot %d (%d,%d,%d) outside the %dx%dx%d model", j, s.sx, s.sy, s.sz, c.nx, c.ny,
+                        c.nz);
+    }
+    CUDA_TRY(cudaSetDevice(device));
+    int rc;
+    if (!tuned && (rc = autotune())) return rc;
+    CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    const int np = npml;
+    std::vector<int4> cells(k);
+    for (int j = 0; j < k; ++j)  // ..vti..:63-65: the source cell is (s - 1) + npml
+        cells[j] = make_int4(shots[j].sx + np - 1, shots[j].sy + np - 1, shots[j].sz + np - 1, 0);
+    CUDA_TRY(cudaMemcpyAsync(d_shots, cells.data(), k * sizeof(int4), cudaMemcpyHostToDevice, st));
+    std::vector<int> mute;
+    if (c.mute) {
+        const size_t ntr = (size_t)c.nx * c.ny;
+        mute.resize(ntr * k);
+        for (int j = 0; j < k; ++j)
+            for (int iy = 0; iy < c.ny; ++iy)
+                for (int ix = 0; ix < c.nx; ++ix)
+                    mute[j * ntr + ix + (size_t)c.nx * iy] =
+                        mute_nt(ix, iy, shots[j].sx, shots[j].sy, shots[j].sz, c.dx, c.dy, c.dz, c.dt, c.fm, v_mute);
+        CUDA_TRY(cudaMemcpyAsync(d_mute, mute.data(), mute.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+    const size_t fb = fstride * esz * (size_t)k;
+    for (void *f : {u, v, w, P, Q, px, py, pz, qx, qy, qz})
+        if (f) CUDA_TRY(cudaMemsetAsync(field_alloc(f, esz), 0, fb, st));
+    K1Launch Lv{}, Ls{};
+    K1Params p{};
+    p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
+    p.nx = c.nx; p.ny = c.ny; p.npml = np;
+    p.dtx = c.dt / c.dx; p.dty = c.dt / c.dy; p.dtz = c.dt / c.dz;
+    const float *q = pml;
+    p.cx1 = q; p.cx2 = q + g.nnx; p.ax1 = q + 2 * g.nnx; p.ax2 = q + 3 * g.nnx; q += 4 * g.nnx;
+    p.cy1 = q; p.cy2 = q + g.nny; p.ay1 = q + 2 * g.nny; p.ay2 = q + 3 * g.nny; q += 4 * g.nny;
+    p.cz1 = q; p.cz2 = q + g.nnz; p.az1 = q + 2 * g.nnz; p.az2 = q + 3 * g.nnz;
+    p.s_x = p.s_y = p.s_z = -100;  // per shot: p.shots
+    p.shots = d_shots;
+    p.fstride = fstride;
+    p.rstride = (size_t)c.nt * c.nx * c.ny;
+    p.taper = taper;
+    p.px = px; p.py = py; p.pz = pz; p.qx = qx; p.qy = qy; p.qz = qz;
+    for (int a = 0; a < 3; ++a) { p.ulo[a] = ulo[a]; p.uhi[a] = uhi[a]; }
+    p.rec = rec;
+    p.mute_nt = c.mute ? d_mute : nullptr;
+    p.nt = c.nt;
+    p.err = d_err;
+    p.svp = sig_v / sig_p;
+    p.spv = sig_p / sig_v;
+    p.rec_scale = 1.0f / sig_p;
+    Lv.kind = K1_VTI_VEL; Ls.kind = K1_VTI_STR;
+    Lv.maps = mvel[tune[0].tx == 16 ? 1 : 0]; Lv.nmaps = nvel;
+    Ls.maps = mstr[tune[1].tx == 16 ? 1 : 0]; Ls.nmaps = nstr;
+    Lv.out0 = u; Lv.out1 = v; Lv.out2 = w;
+    Ls.out0 = P; Ls.out1 = Q;
+    Lv.tx = tune[0].tx; Lv.depth = tune[0].depth; Lv.mode = tune[0].mode; Lv.rows = tune[0].rows;
+    Ls.tx = tune[1].tx; Ls.depth = tune[1].depth; Ls.mode = tune[1].mode; Ls.rows = tune[1].rows;
+    Lv.rot = tune[0].rot; Ls.rot = tune[1].rot;
+    Lv.fp64 = Ls.fp64 = false; Lv.half = Ls.half = half; Lv.grid = Ls.grid = 0;
+    Lv.ms = Ls.ms = 1;
+    Lv.nshot = Ls.nshot = k;
+    if ((rc = prepare_profiling(this, 3))) return rc;
+    rc = timed_loop(this, graph && !profiling, [&]() -> int {
+        for (int it = 0; it < c.nt; ++it) {
+            p.it = it;
+            p.inj = inj[it];
+            p.amp0 = amp0[it] * sig_p;  // exact: sig_p is a power of two
+            p.amp1 = amp1[it] * sig_p;
+            Lv.p = p;
+            Ls.p = p;
+            if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it], st));
+            CUDA_TRY(launch_vti(Lv, st));
+            if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 1], st));
+            CUDA_TRY(launch_vti(Ls, st));
+            if (profiling) CUDA_TRY(cudaEventRecord(kev[3 * it + 2], st));
+        }
+        return A3D_OK;
+    });
+    if (rc) return rc;
+    if ((rc = check_kernel_error(this))) return rc;
+    if (profiling)
+        for (int it = 0; it < c.nt; ++it)
+            for (int kk = 0; kk < 2; ++kk) {
+                float f = 0;
+                CUDA_TRY(cudaEventElapsedTime(&f, kev[3 * it + kk], kev[3 * it + kk + 1]));
+                kms[kk] += f;
+                klaunch[kk] += 1;
+            }
+    if (ms) {
+        float f = 0;
+        CUDA_TRY(cudaEventElapsedTime(&f, ev0, ev1));
+        *ms = f;
+    }
+    return A3D_OK;
+}
+
 // ---------------------------------------------------------------------------
 // C API
 
@@ -1063,6 +1209,8 @@ static int validate(const a3d_config *c) {
         return fail(A3D_E_ARG, "unknown boundary %d", c->boundary);
     if (c->boundary == A3D_BOUNDARY_LEARNED && (c->physics != A3D_ISO || c->storage != A3D_FP32))
         return fail(A3D_E_UNSUPPORTED, "the learned rim is built for the isotropic engine with FP32 storage");
+    if (c->batch > 1 && (c->physics != A3D_VTI || c->storage == A3D_FP64))
+        return fail(A3D_E_UNSUPPORTED, "multi-shot sweeps are built for the VTI engine with FP32 or 2-byte storage");
     return A3D_OK;
 }
 
@@ -1092,6 +1240,7 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
     e->half = cfg->storage == A3D_BF16 ? 1 : (cfg->storage == A3D_FP16 ? 2 : 0);
     e->esz = e->fp64 ? 8 : (e->half ? 2 : 4);
     e->tx = 8;
+    e->nbatch = cfg->batch > 1 ? cfg->batch : 1;
     if (ph == A3D_2ORDER) {
         e->npml = cfg->npml > 0 ? cfg->npml : 50;  // npd, 2O:19
         if (e->cfg.rec_z < 0) e->cfg.rec_z = 1;    // 2O:159 records at model depth 1
@@ -1118,6 +1267,8 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
         delete e;
         return fail(A3D_E_ARG, "padded grid of %zu cells exceeds 2^31 - 1", n);
     }
+    // one copy of a wavefield per shot of a multi-shot sweep, 256-byte aligned
+    e->fstride = (e->g.elems() * e->esz + 255) / 256 * 256 / e->esz;
     if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) {
         delete e;
@@ -1165,6 +1316,29 @@ extern "C" int a3d_engine_run_device(a3d_engine *e, const a3d_shot *shot, float 
     clear_error();
     if (!e || !shot) return fail(A3D_E_ARG, "null engine or shot");
     return e->run(*shot, rec_dev, nullptr, ms);
+}
+
+extern "C" int a3d_engine_run_shots(a3d_engine *e, const a3d_shot *shots, int k, float *recs_host, double *ms) {
+    clear_error();
+    if (!e || !shots) return fail(A3D_E_ARG, "null engine or shots");
+    int rc = e->run_shots(shots, k, ms);
+    if (rc) return rc;
+    if (recs_host) {
+        cudaError_t ce = cudaMemcpy(recs_host, e->rec, (size_t)k * e->cfg.nt * e->cfg.nx * e->cfg.ny * 4,
+                                    cudaMemcpyDeviceToHost);
+        if (ce != cudaSuccess) return fail(A3D_E_CUDA, "record copy failed: %s", cudaGetErrorString(ce));
+    }
+    return A3D_OK;
+}
+
+extern "C" int a3d_engine_copy_record(a3d_engine *e, int j, float *rec_host) {
+    clear_error();
+    if (!e || !rec_host) return fail(A3D_E_ARG, "null engine or buffer");
+    if (j < 0 || j >= e->nbatch) return fail(A3D_E_ARG, "record %d of an engine holding %d", j, e->nbatch);
+    const size_t n = (size_t)e->cfg.nt * e->cfg.nx * e->cfg.ny;
+    CUDA_TRY(cudaSetDevice(e->device));
+    CUDA_TRY(cudaMemcpy(rec_host, e->rec + (size_t)j * n, n * 4, cudaMemcpyDeviceToHost));
+    return A3D_OK;
 }
 
 extern "C" float *a3d_engine_record_device(a3d_engine *e) { return e ? e->rec : nullptr; }

@@ -47,6 +47,12 @@ struct a3d_engine {
     bool fp64 = false;
     int half = 0;          // 2-byte wavefields: 1 bfloat16, 2 float16 (isotropic and VTI engines)
     size_t esz = 4;        // bytes per wavefield element
+    // multi-shot sweeps (VTI, cfg.batch = K > 1): every wavefield and split
+    // component holds K copies fstride elements apart (4-D tensor maps over them),
+    // K records and K mute tables follow each other, d_shots the shots' source cells
+    int nbatch = 1;
+    size_t fstride = 0;
+    int4 *d_shots = nullptr;
     // power-of-two storage scales of 2-byte wavefields: sig_v for u, v, w, sig_p for P
     // and its split components (1 otherwise)
     float sig_v = 1.0f, sig_p = 1.0f;
@@ -141,7 +147,10 @@ struct a3d_engine {
     ~a3d_engine();
     void *dalloc(size_t bytes);  // zeroed; null on failure
     void *dfield(size_t esz);    // zeroed padded field; returns its base (allocation + zoff)
+    // nbatch copies of a wavefield, fstride elements apart; returns the first copy's base
+    void *dfield_batch();
     size_t field_bytes(size_t esz) const { return g.elems() * esz; }
     void *field_alloc(void *base, size_t es) const { return (char *)base - a3d::Grid::zoff * es; }
     int run(const a3d_shot &s, float *rec_dev, const a3d::SnapHook *hook, double *ms);
+    int run_shots(const a3d_shot *shots, int k, double *ms);  // multi-shot sweeps (nbatch > 1)
 };

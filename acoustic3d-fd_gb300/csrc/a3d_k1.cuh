@@ -32,6 +32,12 @@ struct K1Params {
     // terms, spv = sigma_P / sigma_v the pressure terms, rec_scale = 1 / sigma_P
     // the recorded P.  All 1 for 4- and 8-byte storage.
     float svp, spv, rec_scale;
+    // multi-shot sweeps (sw.nshot > 1, VTI): source cell of each shot in padded
+    // coordinates (x, y, z, unused) instead of s_x, s_y, s_z; the shots' wavefields
+    // and split components lie fstride elements apart, their records rstride floats
+    // apart and their mute tables nx * ny ints apart
+    const int4 *shots;
+    size_t fstride, rstride;
 };
 
 enum K1Kind { K1_ISO_VEL = 0, K1_ISO_STR, K1_VTI_VEL, K1_VTI_STR, K1_TTI_VEL, K1_TTI_STR, K1_ISO_STEP };
@@ -53,6 +59,8 @@ struct K1Launch {
     int mode;   // sweep plan (plan_sweep)
     int rows;   // tile rows per consumer warp (iso: 2 or 4; VTI/TTI: 1)
     int rot;    // 1: rotated z-tile order of the sweep (Sweep::rot)
+    int ms;     // 1: multi-shot kernels (VTI: 4-D wavefield maps, p.shots, p.fstride, p.rstride)
+    int nshot;  // multi-shot kernels: shots this launch advances (1 .. the maps' shot count)
 };
 
 cudaError_t launch_k1(const K1Launch &L, cudaStream_t st);
@@ -63,5 +71,6 @@ namespace a3d {
 cudaError_t launch_iso(const K1Launch &L, cudaStream_t st);
 cudaError_t launch_iso_step(const K1Launch &L, cudaStream_t st);  // fused isotropic step (FP32)
 cudaError_t launch_vti(const K1Launch &L, cudaStream_t st);
+cudaError_t launch_vti_ms(const K1Launch &L, cudaStream_t st);  // L.ms (launch_vti forwards)
 cudaError_t launch_tti(const K1Launch &L, cudaStream_t st);
 }  // namespace a3d

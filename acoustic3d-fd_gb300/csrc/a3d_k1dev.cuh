@@ -31,6 +31,7 @@ static cudaError_t k1_launch(Kern kern, int nthreads, size_t smem, long long W, 
 template <int TX, class Kern>
 static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid, int mode, int rot) {
     p.sw.ntz = (p.nnz - 2 * MM + 31) / 32;
+    if (p.sw.nshot < 1) p.sw.nshot = 1;  // multi-shot sweeps set it before the launch
     p.sw.ntx = (p.nnx - 2 * MM + TX - 1) / TX;
     p.sw.y_begin = MM;
     p.sw.NY = p.nny - 2 * MM;
@@ -44,6 +45,26 @@ static int k1_sweep(K1Params &p, Kern kern, int nthreads, size_t smem, int grid,
     const int g = plan_sweep(p.sw, occ, mode);
     p.sw.rot = rot ? 1 : 0;
     return grid > 0 ? grid : g;
+}
+
+// TMA load of a wavefield tile: 3-D, or 4-D with the shot as 4th coordinate in a
+// multi-shot sweep
+template <bool MS>
+__device__ __forceinline__ void tma_field(void *dst, const CUtensorMap *map, uint64_t *bar, int z, int x, int y,
+                                          int shot) {
+    if constexpr (MS) tma_load_4d(dst, map, bar, z, x, y, shot);
+    else tma_load_3d(dst, map, bar, z, x, y);
+}
+
+// source cell of the segment's shot (padded coordinates)
+template <bool MS>
+__device__ __forceinline__ int3 shot_cell(const K1Params &p, int shot) {
+    if constexpr (MS) {
+        const int4 c = p.shots[shot];
+        return make_int3(c.x, c.y, c.z);
+    } else {
+        return make_int3(p.s_x, p.s_y, p.s_z);
+    }
 }
 
 // loads of a stored field value / smem tile element as the arithmetic type

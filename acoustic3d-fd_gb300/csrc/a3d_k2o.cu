@@ -227,6 +227,7 @@ static cudaError_t launch_k2o_t(const K2OLaunch &L, cudaStream_t st) {
     if (cudaError_t e = ensure_smem_attr(kern, SM::TOTAL, attr); e != cudaSuccess) return e;
     K2OParams p = L.p;
     p.sw.ntz = (p.nnz - 2 * MM + 31) / 32;
+    p.sw.nshot = 1;
     p.sw.ntx = (p.nnx - 2 * MM + TX - 1) / TX;
     p.sw.y_begin = MM;
     p.sw.NY = p.nny - 2 * MM;

@@ -26,6 +26,7 @@ namespace a3d {
 // past the pressure planes it outputs).
 struct Seg {
     int tile, ya, yb, z0, x0, oa, ob;
+    int shot;  // shot of a multi-shot sweep (0 otherwise)
 };
 
 template <int TX, int EXT = 0>
@@ -34,7 +35,7 @@ __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long 
     int c = 0;
     if (sw.wave) {  // virtual order of the wave plan (Sweep::wave): this CTA's units
         const long long G = gridDim.x, b = blockIdx.x, NY = sw.NY;
-        const long long T = (long long)sw.ntz * sw.ntx, P = T / G, R = T - P * G;
+        const long long T = (long long)sw.ntz * sw.ntx * sw.nshot, P = T / G, R = T - P * G;
         const long long i = w - (b * P * NY + (b * R * NY) / G);
         long long tile, y;
         if (i < P * NY) {  // whole columns: tile b + k G
@@ -50,7 +51,7 @@ __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long 
         wend = w + (NY - y);  // the column ends
         if (wend > w1) wend = w1;
     } else {
-        const long long full = (long long)sw.ntz * sw.ntx * sw.Yc;  // units of a full chunk
+        const long long full = (long long)sw.ntz * sw.ntx * sw.nshot * sw.Yc;  // units of a full chunk
         c = (int)(w / full);
         const long long r = w - c * full;
         const int len = min(sw.Yc, sw.NY - c * sw.Yc);
@@ -60,8 +61,10 @@ __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long 
         if (wend > w1) wend = w1;
     }
     s.yb = s.ya + (int)(wend - w);
-    int zt = s.tile % sw.ntz;
-    const int xt = s.tile / sw.ntz;
+    s.shot = s.tile % sw.nshot;
+    const int gt = s.tile / sw.nshot;  // tile of the grid
+    int zt = gt % sw.ntz;
+    const int xt = gt / sw.ntz;
     if (sw.rot) {
         const long long nch = (sw.NY + sw.Yc - 1) / sw.Yc, col = (long long)c * sw.ntx + xt;
         zt = (int)((zt + col * sw.ntz / (nch * sw.ntx)) % sw.ntz);

@@ -464,6 +464,90 @@ def run_windows(args):
     print(json.dumps(line), flush=True)
 
 
+def run_vti_batch(args):
+    """VTI survey of the 384 x 384 x 256 model (the vti384 workload) in multi-shot
+    sweeps: a bench step is one launch sequence advancing --batch shots of the 8 x 8
+    surface shot grid (x, y in 24 + 48 i, depth 2) through all nt = 2500 steps.
+    value = updated cells x nt x shots / device time; beside it the same model's
+    single-shot FP32 path (one shot per run, as the reference runs them), the
+    shots/hour of both and their ratio, and the record error against FP64 of the
+    sweep's first shot and of the single FP32 shot."""
+    import a3d
+    import build as pkg_build
+    import synthetic as S
+    pkg_build.build()
+    cfgd, models, _, meta = workload("vti384", args.nt or None)
+    K = max(1, args.batch)
+    shots = S.vti_shot_grid()[:K]
+    nt = cfgd["nt"]
+    cells = updated_cells(cfgd)
+
+    def cfg_of(storage, batch=0):
+        return a3d.make_config("vti", cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"],
+                               dz=cfgd["dz"], nt=nt, dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
+                               storage=storage, batch=batch)
+    # the single-shot FP32 path on the same model and first shot
+    e1 = a3d.Engine(cfg_of(a3d.FP32), models)
+    e1.run_device(*shots[0])
+    single_ms = e1.run_device(*shots[0])
+    rec32 = e1.run(*shots[0]) if not args.no_fp64 else None
+    e1.close()
+    # the multi-shot sweeps
+    eb = a3d.Engine(cfg_of(STORAGE[args.storage], K), models)
+    for _ in range(args.warmup):
+        eb.run_shots(shots, to_host=False)
+    eb.set_profiling(True)
+    dev_ms = 0.0
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            dev_ms += eb.run_shots(shots, with_time=True, to_host=False)[1]
+        wall = time.perf_counter() - t0
+    kms, kn = eb.kernel_times()
+    desc = eb.describe()
+    rec_b = eb.record(0) if not args.no_fp64 else None
+    dev_bytes = eb.device_bytes()
+    eb.close()
+    err = {}
+    if not args.no_fp64:
+        e64 = a3d.Engine(cfg_of(a3d.FP64), models)
+        rec64 = e64.run(*shots[0]).astype(np.float64)
+        e64.close()
+        n64 = np.linalg.norm(rec64.ravel())
+        err = {"sweep_shot0": float(np.linalg.norm((rec_b - rec64).ravel()) / n64),
+               "single_fp32_shot0": float(np.linalg.norm((rec32 - rec64).ravel()) / n64)}
+    ms_step = dev_ms / args.steps
+    value = cells * nt * K * args.steps / (dev_ms / 1000.0) / 1e9
+    sph = 3600.0 * 1000.0 * K / ms_step
+    sph1 = 3600.0 * 1000.0 / single_ms
+    peak, peak_kind = measured_peak()
+    es = 4 if args.storage == "fp32" else 2
+    # compulsory bytes per cell and shot: wavefields read and written per shot, the
+    # model parameters once per tile for the whole sweep (1/rho in the velocity
+    # sweep; rho, vp, epsilon, delta in the stress sweep)
+    kb = (es * 8 + 4.0 / K, es * 7 + 16.0 / K)
+    per = [kms[i] / kn[i] if kn[i] else 0.0 for i in range(2)]
+    dom = 0 if per[0] >= per[1] else 1
+    achieved = kb[dom] * cells * K / (per[dom] / 1000.0) / 1e9
+    line = {"metric": "Gpts/s", "value": value, "unit": "Gpts/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if es == 4 else f"f32 arithmetic, {args.storage} wavefields",
+            "data": "synthetic",
+            "config": dict(meta, workload="vti1order_384x384x256_nt%d_sweep%d" % (nt, K),
+                           shots=[list(x) for x in shots], batch=K, storage=args.storage, parallelism="replicas1",
+                           l2="inputs larger than L2: %d MB of wavefields and model per shot" %
+                              (dev_bytes // K // 2**20)),
+            "shots_per_hour": sph, "single_shot_fp32": {"ms_per_shot": single_ms, "shots_per_hour": sph1},
+            "shots_per_hour_ratio": sph / sph1, "rel_l2_vs_fp64": err,
+            "roofline": {"bound": "hbm", "kernel": ("vti_vel", "vti_stress")[dom], "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "peak_source": peak_kind, "bytes_per_cell_and_shot": kb[dom],
+                         "kernel_ms_per_launch": per[dom]},
+            "device_bytes": dev_bytes, "wall_s_timed": wall, "clocks": clk.summary(),
+            "tuning": desc.get("kernels"), "gpu_launches": int(kn[0] + kn[1])}
+    print(json.dumps(line), flush=True)
+
+
 def run_learned(args):
     """The learned absorbing rim against the PML (isotropic 256^3, d 10 m, nt 2000,
     20 Hz Ricker at the centre, depth 8): a bench step is one learned-rim shot
@@ -523,7 +607,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="iso256",
-                    choices=["iso256", "2o128", "2o128lit", "vti384", "tti256", "ttiwin", "learned"])
+                    choices=["iso256", "2o128", "2o128lit", "vti384", "vti384batch", "tti256", "ttiwin",
+                             "learned"])
+    ap.add_argument("--batch", type=int, default=32, help="vti384batch: shots per multi-shot sweep")
     ap.add_argument("--params", default="", help="learned: closure weights (.npy; default the package's)")
     ap.add_argument("--windows", type=int, default=4, help="ttiwin: apertures per bench step (of 48)")
     ap.add_argument("--nt", type=int, default=0, help="override nt (profiling runs only)")
@@ -535,13 +621,20 @@ def main():
     ap.add_argument("--storage", default="fp32", choices=list(STORAGE),
                     help="wavefield storage (bf16 / fp16: isotropic and VTI engines; arithmetic stays fp32)")
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    # three warm-up steps at least for the shot workloads; a multi-shot sweep of the
+    # batched survey is itself 30-120 s of device time, after the autotuner has run
+    # every kernel, so one warm-up sweep is allowed there
+    if args.impl == "ours" and args.workload != "vti384batch":
+        args.warmup = max(args.warmup, 3)
 
     if args.workload == "ttiwin":
         run_windows(args)
         return
     if args.workload == "learned":
         run_learned(args)
+        return
+    if args.workload == "vti384batch":
+        run_vti_batch(args)
         return
     cfgd, models, shot, meta = workload(args.workload, args.nt or None)
     meta["storage"] = args.storage

@@ -110,6 +110,10 @@ typedef struct {
                           absorber) or A3D_BOUNDARY_LEARNED (isotropic, FP32: a 6-cell
                           undamped rim corrected by the closure set with
                           a3d_engine_set_closure; npml must be 10 or <= 0)          */
+    int batch;         /* VTI, FP32 / BF16 / FP16: the most shots one launch advances
+                          together (multi-shot sweeps, a3d_engine_run_shots); the
+                          engine holds that many copies of every wavefield and
+                          record.  <= 1: one shot per launch                        */
 } a3d_config;
 
 enum a3d_boundary { A3D_BOUNDARY_PML = 0, A3D_BOUNDARY_LEARNED = 1 };
@@ -139,7 +143,23 @@ int a3d_engine_run(a3d_engine *e, const a3d_shot *shot, float *rec_host, int sna
  * nt*nx*ny floats (or NULL to keep the engine's own buffer); no host copies. */
 int a3d_engine_run_device(a3d_engine *e, const a3d_shot *shot, float *rec_dev, double *ms);
 
-/* Device pointer of the engine's record buffer ([ny][nx][nt] floats). */
+/* Multi-shot sweeps: no counterpart in the reference, which runs one shot per
+ * library call in its own process (readmodel.py:186-204; each call a full
+ * cuda_3dfd_vti, ..vti..:389-688).  On an engine created with cfg.batch = K > 1,
+ * run k <= K shots of the same model together: every launch advances all k shots
+ * by one step, the CTAs that hold one tile of the grid for the different shots run
+ * side by side, so each tile's model parameters come from HBM once per step for
+ * all shots.  Each shot's record equals its one-shot run (a3d_engine_run) bit for
+ * bit.  recs_host: k * nt*nx*ny floats, shot after shot (or NULL); *ms (optional)
+ * the device time of the whole time loop.  Snapshots are not taken. */
+int a3d_engine_run_shots(a3d_engine *e, const a3d_shot *shots, int k, float *recs_host, double *ms);
+
+/* Copy the record of shot j (0-based, in the order of the last run's shots; 0 for
+ * a one-shot run) to rec_host (nt*nx*ny floats). */
+int a3d_engine_copy_record(a3d_engine *e, int j, float *rec_host);
+
+/* Device pointer of the engine's record buffer ([ny][nx][nt] floats; an engine
+ * with cfg.batch = K holds K of them, shot after shot). */
 float *a3d_engine_record_device(a3d_engine *e);
 
 /* Bytes the engine holds in device memory. */
@@ -179,7 +199,8 @@ typedef struct {
     float *recs_host;           /* out (or NULL): the records one after another, shot i
                                    taking nt * wnx * wny floats ([wny][wnx][nt])        */
     size_t *rec_offsets;        /* out (or NULL): nshot float offsets into recs_host   */
-    double *ms;                 /* out (or NULL): nshot device times of the time loops */
+    double *ms;                 /* out (or NULL): nshot device times of the time loops
+                                   (a multi-shot sweep's time shared evenly by its shots) */
 } a3d_opts;
 
 /* Run nshot shots.  Returns A3D_OK, or the first failure (later shots not run). */
