@@ -199,6 +199,12 @@ __global__ void pad_field(const float *__restrict__ m, float *__restrict__ out, 
                 v = m[(size_t)cz + (size_t)nz * ((size_t)cx + (size_t)nx * cy)];
                 if (mode == 1) v = v != 0.0f ? 1.0f / v : 0.0f;
                 else if (mode == 2) { const float t = v * sc; v = t * t; }
+                else if (mode == 3) {  // times 0.5 (1 + cos(pi d / sc)), d = cells into the absorber
+                    const int d = max(max(max(pad - iz, iz - (pad + nz - 1)), max(pad - ix, ix - (pad + nx - 1))),
+                                      max(max(pad - iy, iy - (pad + ny - 1)), 0));
+                    const float r = fminf((float)d / sc, 1.0f);
+                    v = v * (0.5f + 0.5f * cospif(r));
+                }
             }
         }
         out[i] = v;
@@ -325,8 +331,13 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
         CUDA_TRY(cudaDeviceSynchronize());
     }
     if (c.physics != A3D_ISO) {
-        if ((rc = upload_model(e, eps, &e->eps, raw))) return rc;
-        if ((rc = upload_model(e, del, &e->del, raw))) return rc;
+        // A3D_ANISO_PML_TAPER=1: epsilon and delta fall to 0 across the absorber
+        // (cosine ramp over npml - 4 cells); off by default
+        const char *tp = getenv("A3D_ANISO_PML_TAPER");
+        const int tmode = tp && tp[0] == '1' ? 3 : 0;
+        const float tw = (float)std::max(1, e->npml - MM);
+        if ((rc = upload_model(e, eps, &e->eps, raw, tmode, tw))) return rc;
+        if ((rc = upload_model(e, del, &e->del, raw, tmode, tw))) return rc;
     }
     if (c.physics == A3D_TTI) {
         // cos/sin of tilt and azimuth in float on the host (libm, as the oracle and
