@@ -479,6 +479,12 @@ def run_vti_batch(args):
     cfgd, models, _, meta = workload("vti384", args.nt or None)
     K = max(1, args.batch)
     shots = S.vti_shot_grid()[:K]
+    if args.scale > 1:  # a smaller case of the same workload (profiling): every axis / scale
+        f = args.scale
+        cfgd = dict(cfgd, nx=cfgd["nx"] // f, ny=cfgd["ny"] // f, nz=cfgd["nz"] // f)
+        models = S.vti_model(cfgd["nx"], cfgd["ny"], cfgd["nz"], 4500.0)
+        shots = S.vti_shot_grid(first=24 // f, step=48 // f)[:K]
+        meta = dict(meta, model="%dx%dx%d" % (cfgd["nx"], cfgd["ny"], cfgd["nz"]))
     nt = cfgd["nt"]
     cells = updated_cells(cfgd)
 
@@ -533,7 +539,7 @@ def run_vti_batch(args):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if es == 4 else f"f32 arithmetic, {args.storage} wavefields",
             "data": "synthetic",
-            "config": dict(meta, workload="vti1order_384x384x256_nt%d_sweep%d" % (nt, K),
+            "config": dict(meta, workload="vti1order_%s_nt%d_sweep%d" % (meta["model"], nt, K),
                            shots=[list(x) for x in shots], batch=K, storage=args.storage, parallelism="replicas1",
                            l2="inputs larger than L2: %d MB of wavefields and model per shot" %
                               (dev_bytes // K // 2**20)),
@@ -610,6 +616,7 @@ def main():
                     choices=["iso256", "2o128", "2o128lit", "vti384", "vti384batch", "tti256", "ttiwin",
                              "learned"])
     ap.add_argument("--batch", type=int, default=32, help="vti384batch: shots per multi-shot sweep")
+    ap.add_argument("--scale", type=int, default=1, help="vti384batch: divide every model axis (profiling cases)")
     ap.add_argument("--params", default="", help="learned: closure weights (.npy; default the package's)")
     ap.add_argument("--windows", type=int, default=4, help="ttiwin: apertures per bench step (of 48)")
     ap.add_argument("--nt", type=int, default=0, help="override nt (profiling runs only)")
