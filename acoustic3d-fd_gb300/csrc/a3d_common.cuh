@@ -187,14 +187,19 @@ __device__ __forceinline__ void consumer_sync(int nthreads) {
 // then split into gridDim.x contiguous ranges of nearly equal length.  With one
 // chunk-segment per CTA (the host picks Yc so), CTAs that run concurrently march
 // the same y range and neighbouring tiles read each other's halos from L2.
-// A sweep over several shots of one model (nshot > 1) takes the shot as the
-// fastest part of the tile index, so the CTAs that hold one tile of the grid for
-// the different shots run at the same time and read its model parameters once
-// from HBM, the others from L2.
+// A sweep over several shots of one model (nshot > 1) orders its tiles in blocks
+// of sblk grid tiles, each block visited for every shot before the next block:
+//     tile = t_in_block + sblk * (shot + nshot * block)
+// (the last block may hold fewer tiles).  With sblk = 1 the shot is the fastest
+// part, so the CTAs that hold one grid tile for the different shots run at the
+// same time and read its model parameters once from HBM, the others from L2; with
+// larger blocks the CTAs that run together also hold neighbouring tiles of one
+// shot and share their halo rows through L2.  The autotuner picks sblk.
 
 struct Sweep {
     int ntz, ntx;    // tiles along z and x
     int nshot;       // shots advanced together (>= 1)
+    int sblk;        // multi-shot sweeps: grid tiles per block of the tile order (<= 1: one)
     int y_begin;     // first output plane
     int NY;          // output planes per tile
     int Yc;          // planes per y chunk

@@ -199,12 +199,6 @@ __global__ void pad_field(const float *__restrict__ m, float *__restrict__ out, 
                 v = m[(size_t)cz + (size_t)nz * ((size_t)cx + (size_t)nx * cy)];
                 if (mode == 1) v = v != 0.0f ? 1.0f / v : 0.0f;
                 else if (mode == 2) { const float t = v * sc; v = t * t; }
-                else if (mode == 3) {  // times 0.5 (1 + cos(pi d / sc)), d = cells into the absorber
-                    const int d = max(max(max(pad - iz, iz - (pad + nz - 1)), max(pad - ix, ix - (pad + nx - 1))),
-                                      max(max(pad - iy, iy - (pad + ny - 1)), 0));
-                    const float r = fminf((float)d / sc, 1.0f);
-                    v = v * (0.5f + 0.5f * cospif(r));
-                }
             }
         }
         out[i] = v;
@@ -331,13 +325,8 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
         CUDA_TRY(cudaDeviceSynchronize());
     }
     if (c.physics != A3D_ISO) {
-        // A3D_ANISO_PML_TAPER=1: epsilon and delta fall to 0 across the absorber
-        // (cosine ramp over npml - 4 cells); off by default
-        const char *tp = getenv("A3D_ANISO_PML_TAPER");
-        const int tmode = tp && tp[0] == '1' ? 3 : 0;
-        const float tw = (float)std::max(1, e->npml - MM);
-        if ((rc = upload_model(e, eps, &e->eps, raw, tmode, tw))) return rc;
-        if ((rc = upload_model(e, del, &e->del, raw, tmode, tw))) return rc;
+        if ((rc = upload_model(e, eps, &e->eps, raw))) return rc;
+        if ((rc = upload_model(e, del, &e->del, raw))) return rc;
     }
     if (c.physics == A3D_TTI) {
         // cos/sin of tilt and azimuth in float on the host (libm, as the oracle and
@@ -642,15 +631,22 @@ int a3d_engine::autotune_form() {
                 depth < 0 || depth > maxdepth || (fused && rows == 4) ||
                 (rows != 1 && rows != 2 && rows != 4) || (rows == 4 && tx != 16) || mode < 0 || mode > 2)
                 return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[,rot][;...], got \"%s\"", env);
+            int sblk = 1, n3 = 0;
             if (q[n] == ',') {
                 if (sscanf(q + n + 1, "%d%n", &rot, &n2) != 1 || rot < 0 || rot > 1)
-                    return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[,rot][;...], got \"%s\"", env);
+                    return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[,rot[,sblk]][;...], got \"%s\"", env);
                 n += 1 + n2;
+                if (q[n] == ',') {  // tile block of a multi-shot sweep
+                    if (sscanf(q + n + 1, "%d%n", &sblk, &n3) != 1 || sblk < 1)
+                        return fail(A3D_E_ARG, "A3D_TUNE: expected tx,rows,depth,plan[,rot[,sblk]][;...], got \"%s\"", env);
+                    n += 1 + n3;
+                }
             }
             if (!multirow && rows != 1) return fail(A3D_E_ARG, "A3D_TUNE: this physics runs one row per warp");
             tune[k] = Tune{tx, depth, mode, rows};
             tune[k].ms = 0;
             tune[k].rot = c.physics == A3D_2ORDER ? 0 : rot;
+            tune[k].sblk = sblk;
             q += n;
             if (*q == ';') ++q;
             else if (k == 0) { tune[1] = tune[0]; break; }
@@ -712,6 +708,7 @@ int a3d_engine::autotune_form() {
         if (nbatch > 1) {  // multi-shot kernels over every copy (no source: d_shots lie outside)
             L.ms = 1;
             L.nshot = nbatch;
+            L.sblk = tc.sblk;
             p.shots = d_shots;
             p.fstride = fstride;
             p.rstride = (size_t)c.nt * c.nx * c.ny;
@@ -775,6 +772,21 @@ int a3d_engine::autotune_form() {
                 r.rot = 1;
                 fin.push_back(r);
             }
+        }
+        if (nbatch > 1) {  // multi-shot sweeps: each finalist with tile blocks of 1, one x
+            // column, 4 and 16 columns, and the whole grid (Sweep::sblk)
+            const int ntz = (g.nnz - 2 * MM + 31) / 32;
+            std::vector<Tune> more;
+            for (const Tune &f : fin) {
+                const int T = ntz * ((g.nnx - 2 * MM + f.tx - 1) / f.tx);
+                for (int b : {1, ntz, 4 * ntz, 16 * ntz, T}) {
+                    if (b > T && b != T) continue;
+                    Tune t = f;
+                    t.sblk = b;
+                    more.push_back(t);
+                }
+            }
+            fin.swap(more);
         }
         const Tune other = kinds == 2 ? tune[1 - k] : Tune{};
         float best = 1e30f;
@@ -1182,6 +1194,8 @@ int a3d_engine::run_shots(const a3d_shot *shots, int k, double *ms) {
     Lv.fp64 = Ls.fp64 = false; Lv.half = Ls.half = half; Lv.grid = Ls.grid = 0;
     Lv.ms = Ls.ms = 1;
     Lv.nshot = Ls.nshot = k;
+    Lv.sblk = tune[0].sblk;
+    Ls.sblk = tune[1].sblk;
     if ((rc = prepare_profiling(this, 3))) return rc;
     rc = timed_loop(this, graph && !profiling, [&]() -> int {
         for (int it = 0; it < c.nt; ++it) {
@@ -1484,11 +1498,12 @@ extern "C" int a3d_engine_describe(a3d_engine *e, char *buf, size_t n) {
     }
     snprintf(buf, n,
              "{\"grid\": [%d, %d, %d], \"ldz\": %d, \"pad\": %d, \"device_bytes\": %zu, \"fused\": %d, "
-             "\"kernels\": [{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"rot\": %d, \"ms\": %.4f}, "
-             "{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"rot\": %d, \"ms\": %.4f}]}",
+             "\"kernels\": [{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"rot\": %d, \"sblk\": %d, "
+             "\"ms\": %.4f}, {\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"rot\": %d, \"sblk\": %d, "
+             "\"ms\": %.4f}]}",
              e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, (int)e->fused, e->tune[0].tx, e->tune[0].rows,
-             e->tune[0].depth, e->tune[0].mode, e->tune[0].rot, e->tune[0].ms, e->tune[1].tx, e->tune[1].rows,
-             e->tune[1].depth, e->tune[1].mode, e->tune[1].rot, e->tune[1].ms);
+             e->tune[0].depth, e->tune[0].mode, e->tune[0].rot, e->tune[0].sblk, e->tune[0].ms, e->tune[1].tx,
+             e->tune[1].rows, e->tune[1].depth, e->tune[1].mode, e->tune[1].rot, e->tune[1].sblk, e->tune[1].ms);
     return A3D_OK;
 }
 

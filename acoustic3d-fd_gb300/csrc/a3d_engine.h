@@ -109,7 +109,7 @@ struct a3d_engine {
 
     // launch configuration per kernel kind ([0] velocity / 2nd-order step, [1] stress),
     // chosen by the autotuner on the first run unless fixed by the config
-    struct Tune { int tx = 8; int depth = 0; int mode = 0; int rows = 2; float ms = 0; int rot = 0; };
+    struct Tune { int tx = 8; int depth = 0; int mode = 0; int rows = 2; float ms = 0; int rot = 0; int sblk = 1; };
     Tune tune[2];
     bool tuned = false;
     int autotune();

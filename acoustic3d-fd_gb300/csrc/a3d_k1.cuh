@@ -61,6 +61,7 @@ struct K1Launch {
     int rot;    // 1: rotated z-tile order of the sweep (Sweep::rot)
     int ms;     // 1: multi-shot kernels (VTI: 4-D wavefield maps, p.shots, p.fstride, p.rstride)
     int nshot;  // multi-shot kernels: shots this launch advances (1 .. the maps' shot count)
+    int sblk;   // multi-shot kernels: grid tiles per block of the tile order (Sweep::sblk)
 };
 
 cudaError_t launch_k1(const K1Launch &L, cudaStream_t st);

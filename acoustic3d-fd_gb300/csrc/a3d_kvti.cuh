@@ -538,6 +538,7 @@ template <int TX, class S, int D, int R, bool MS>
 static inline cudaError_t launch_vti_s(const K1Launch &L, cudaStream_t st) {
     K1Params p = L.p;
     p.sw.nshot = MS ? (L.nshot > 1 ? L.nshot : 1) : 1;
+    p.sw.sblk = MS ? L.sblk : 1;
     constexpr int NT = 32 * (TX / (2 * R) + 1);
     if (L.kind == K1_VTI_VEL) {
         static SmemAttr attr;

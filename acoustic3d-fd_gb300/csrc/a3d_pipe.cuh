@@ -61,8 +61,24 @@ __device__ __forceinline__ Seg make_seg(const Sweep &sw, long long w, long long 
         if (wend > w1) wend = w1;
     }
     s.yb = s.ya + (int)(wend - w);
-    s.shot = s.tile % sw.nshot;
-    const int gt = s.tile / sw.nshot;  // tile of the grid
+    int gt;  // tile of the grid
+    if (sw.nshot <= 1) {
+        s.shot = 0;
+        gt = s.tile;
+    } else {  // blocks of B grid tiles, each visited for every shot (Sweep::sblk)
+        const long long T = (long long)sw.ntz * sw.ntx;
+        const long long B = sw.sblk > 1 ? (sw.sblk < T ? sw.sblk : T) : 1;
+        const long long v = s.tile, span = B * sw.nshot, nfull = T / B;
+        if (v < nfull * span) {
+            const long long r = v % span;
+            s.shot = (int)(r / B);
+            gt = (int)((v / span) * B + r % B);
+        } else {  // the last, shorter block
+            const long long r = v - nfull * span, tl = T - nfull * B;
+            s.shot = (int)(r / tl);
+            gt = (int)(nfull * B + r % tl);
+        }
+    }
     int zt = gt % sw.ntz;
     const int xt = gt / sw.ntz;
     if (sw.rot) {

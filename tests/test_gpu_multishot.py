@@ -73,6 +73,9 @@ def _ms_configs():
             for plan in (0, 1, 2):
                 out.append(f"{tx},{rows},{depth},{plan}")
         out.append(f"{tx},{rows},0,0,1")  # rotated z-tile order
+        for sblk in (3, 7, 10000):  # tile blocks (Sweep::sblk): partial last block, one past the grid
+            out.append(f"{tx},{rows},0,2,0,{sblk}")
+            out.append(f"{tx},{rows},2,0,1,{sblk}")
     return out
 
 
