@@ -5,7 +5,9 @@ float16 (float16 with power-of-two per-field scales); every stencil operation an
 the time integration stay float.  There is no bitwise reference for these runs:
 the record is compared with the same shot run in FP64 storage, and the tolerances
 are the stated error of each form on this case (measured on GB300: bfloat16 4.7e-2,
-float16 4.4e-3, FP32 7.7e-7), with about 2x headroom.
+float16 4.4e-3, FP32 7.7e-7), with about 2x headroom.  These bounds are regression
+guards for the 2-byte forms, not the 1e-3 precision target: no 2-byte form meets
+that target, and already this 300-step case puts float16 above it.
 """
 import numpy as np
 import pytest
