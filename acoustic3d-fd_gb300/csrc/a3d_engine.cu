@@ -205,14 +205,6 @@ __global__ void pad_field(const float *__restrict__ m, float *__restrict__ out, 
     }
 }
 
-// out = (rho * vp) * vp elementwise over a padded allocation (two float products,
-// the reference's ((1 * rho) * vp) * vp off the PML, ..iso..:182-184)
-__global__ void rho_vp2(const float *__restrict__ rho, const float *__restrict__ vp, float *__restrict__ out,
-                        size_t elems) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < elems; i += (size_t)gridDim.x * blockDim.x)
-        out[i] = (rho[i] * vp[i]) * vp[i];
-}
-
 // upload a model (nx*ny*nz host floats) into a new padded field; raw: a device
 // scratch buffer of the model's size; m == nullptr pads what raw already holds
 static int upload_model(a3d_engine *e, const float *m, float **dst, float *raw, int mode = 0, float sc = 0.0f) {
@@ -315,14 +307,6 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
         if ((rc = upload_model(e, rho, &e->rho, raw))) return rc;
         // the velocity sweeps multiply by 1/rho (float reciprocal) of the rho just uploaded
         if ((rc = upload_model(e, nullptr, &e->rinv, raw, 1))) return rc;
-    }
-    if (c.physics == A3D_ISO) {
-        e->kvv = (float *)e->dfield(4);
-        if (!e->kvv) return fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", e->field_bytes(4));
-        rho_vp2<<<1024, 256>>>((const float *)e->field_alloc(e->rho, 4), (const float *)e->field_alloc(e->vp, 4),
-                               (float *)e->field_alloc(e->kvv, 4), g.elems());
-        CUDA_TRY(cudaGetLastError());
-        CUDA_TRY(cudaDeviceSynchronize());
     }
     if (c.physics != A3D_ISO) {
         if ((rc = upload_model(e, eps, &e->eps, raw))) return rc;
@@ -452,12 +436,12 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
             (rc = mk(&mvel[2], e->v, true, BOX_CORE)) || (rc = mk(&mvel[3], e->w, true, BOX_CORE)) ||
             (rc = mk(&mvel[4], e->rinv, false, BOX_CORE)))
             return rc;
-        e->nstr = 10;
+        e->nstr = 9;
         if ((rc = mk(&mstr[0], e->v, true, BOX_CORE)) || (rc = mk(&mstr[1], e->u, true, BOX_HX)) ||
             (rc = mk(&mstr[2], e->w, true, BOX_HZ)) || (rc = mk(&mstr[3], e->P, true, BOX_CORE)) ||
             (rc = mk(&mstr[4], e->rho, false, BOX_CORE)) || (rc = mk(&mstr[5], e->vp, false, BOX_CORE)) ||
             (rc = mk(&mstr[6], e->px, true, BOX_CORE)) || (rc = mk(&mstr[7], e->py, true, BOX_CORE)) ||
-            (rc = mk(&mstr[8], e->pz, true, BOX_CORE)) || (rc = mk(&mstr[9], e->kvv, false, BOX_CORE)))
+            (rc = mk(&mstr[8], e->pz, true, BOX_CORE)))
             return rc;
         for (int b = 0; b < 2 && e->fused_ok; ++b) {  // fused step reading set b
             CUtensorMap *ms = e->mstep[t][b];

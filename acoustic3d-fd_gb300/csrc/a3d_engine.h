@@ -64,7 +64,6 @@ struct a3d_engine {
 
     // model parameters on the device (float, padded layout)
     float *vv = nullptr, *vp = nullptr, *rho = nullptr, *rinv = nullptr, *eps = nullptr, *del = nullptr;
-    float *kvv = nullptr;  // isotropic: (rho vp) vp, read by the stress sweep off the PML
     float *tct = nullptr, *tst = nullptr, *tcp = nullptr, *tsp = nullptr;  // TTI trig
     float v_mute = 0.0f;   // direct-wave mute velocity
 

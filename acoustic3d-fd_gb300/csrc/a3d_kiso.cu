@@ -8,9 +8,6 @@
 //   iso_stress: P <- P - rho v^2 dt (D-u/dx + D-v/dy + D-w/dz) (..iso..:145-190)
 //               with split components kept only on PML-damped axes, the receiver
 //               gather at model depth 0 (..iso..:294-304) and the mute fused.
-//               Off the PML it reads one parameter, K = (rho vp) vp precomputed in
-//               float (the reference's ((a1 rho) vp) vp with a1 == 1 exactly); on
-//               items that touch a damped axis it reads rho and vp.
 // Each consumer warp owns R consecutive x rows of the 32 x TX tile (lane = z), so
 // the per-plane pipeline work is shared by R cells and the x-derivative reads
 // R + 7 tile rows instead of 8 R.
@@ -207,22 +204,16 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
 
 // ===========================================================================
 // iso_stress: maps {v (core), u (box HX), w (box HZ), P (core), rho, vp (core, float),
-//                   px, py, pz (core; loaded only for tiles/planes on a damped axis),
-//                   K = (rho vp) vp (core, float)}
+//                   px, py, pz (core; loaded only for tiles/planes on a damped axis)}
 template <int TX, class S, int D>
 struct IsoStrL {
     static constexpr uint32_t C = 32 * TX;
     static constexpr uint32_t UX = 32 * (TX + 8), WZ = ZHalo<S>::W * TX;  // w tile: [TX][W], z halo ZH
     static constexpr uint32_t A_BYTES = C * sizeof(S);
-    // K precomputed (float storage types); the FP64 run forms rho vp vp in double
-    static constexpr bool KP = sizeof(S) != 8;
-    // fixed part of a B item: u, w, P and the first parameter tile (K on items off
-    // the PML, rho on damped ones; always rho without KP); damped items (every item
-    // without KP) add vp, then one split tile per damped axis
-    static constexpr uint32_t B_FIXED = (UX + WZ + C) * sizeof(S) + C * 4;
-    static constexpr uint32_t PAR2 = C * 4;
+    // fixed part of a B item (u, w, P, rho, vp), then one tile per damped axis
+    static constexpr uint32_t B_FIXED = (UX + WZ + C) * sizeof(S) + 2 * C * 4;
     static constexpr uint32_t AUX = C * sizeof(S);
-    static constexpr uint32_t B_BYTES = B_FIXED + PAR2 + 3 * AUX;
+    static constexpr uint32_t B_BYTES = B_FIXED + 3 * AUX;
     static constexpr size_t A_STRIDE = (A_BYTES + 127) / 128 * 128;
     static constexpr size_t B_STRIDE = (B_BYTES + 127) / 128 * 128;
     static_assert(B_FIXED % 128 == 0 && AUX % 128 == 0, "B item parts are 128-byte aligned");
@@ -234,7 +225,7 @@ struct IsoStrL {
 
 template <int TX, class S, int D, int R>
 __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
-    iso_stress(const __grid_constant__ Maps<10> mp, S *__restrict__ P,
+    iso_stress(const __grid_constant__ Maps<9> mp, S *__restrict__ P,
                const __grid_constant__ K1Params p) {
     using L = IsoStrL<TX, S, D>;
     using T = typename Arith<S>::T;
@@ -252,26 +243,22 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     if (w0 >= w1) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr size_t oW = L::UX * sizeof(S), oP = (L::UX + L::WZ) * sizeof(S),
-                     oR = (L::UX + L::WZ + L::C) * sizeof(S),  // K, or rho on damped items
-                     oV = oR + L::C * 4;                        // vp on damped items, then splits
+                     oR = (L::UX + L::WZ + L::C) * sizeof(S), oV = oR + L::C * 4,
+                     oX = L::B_FIXED;  // px, py, pz tiles follow the fixed part
     constexpr uint32_t AUX = L::AUX;
 
     if (warp == NW) {  // producer warp: one thread issues every copy
         if (lane != 0) return;
-        for (int i = 0; i < 10; ++i) prefetch_tmap(&mp.m[i]);
+        for (int i = 0; i < 9; ++i) prefetch_tmap(&mp.m[i]);
         // split components only for tiles / planes on a damped axis, packed after the
-        // parameter tiles in x, y, z order
+        // fixed part in x, y, z order
         auto naux = [&](const Seg &s, int o) {
             return (uint32_t)range_damped(s.x0, TX, p.ulo[0], p.uhi[0]) +
                    (uint32_t)range_damped(o, 1, p.ulo[1], p.uhi[1]) +
                    (uint32_t)range_damped(s.z0, 32, p.ulo[2], p.uhi[2]);
         };
         pipe_produce_m<TX, L::KA, L::KB, L::RB>(
-            p.sw, w0, w1, bars, ringB, p.err,
-            [&](const Seg &s, int o) {
-                const uint32_t na = naux(s, o);
-                return L::B_FIXED + ((na || !L::KP) ? L::PAR2 : 0u) + AUX * na;
-            },
+            p.sw, w0, w1, bars, ringB, p.err, [&](const Seg &s, int o) { return L::B_FIXED + AUX * naux(s, o); },
             [&](uint32_t sa, unsigned char *dst, uint32_t bbytes, uint64_t *bar, const Seg &s, int q) {
                 mbar_arrive_expect_tx(bar, L::A_BYTES + bbytes);
                 tma_load_3d(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0 + ZS, s.x0, q);
@@ -280,14 +267,9 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 tma_load_3d(dst, &mp.m[1], bar, s.z0 + ZS, s.x0 - MM, o);
                 tma_load_3d(dst + oW, &mp.m[2], bar, s.z0 - ZHalo<S>::ZH + ZS, s.x0, o);
                 tma_load_3d(dst + oP, &mp.m[3], bar, s.z0 + ZS, s.x0, o);
-                const bool pd = !L::KP || naux(s, o) != 0;  // rho and vp, or K
-                if (pd) {
-                    tma_load_3d(dst + oR, &mp.m[4], bar, s.z0, s.x0, o);
-                    tma_load_3d(dst + oV, &mp.m[5], bar, s.z0, s.x0, o);
-                } else {
-                    tma_load_3d(dst + oR, &mp.m[9], bar, s.z0, s.x0, o);
-                }
-                unsigned char *ax = dst + oV + L::PAR2;
+                tma_load_3d(dst + oR, &mp.m[4], bar, s.z0, s.x0, o);
+                tma_load_3d(dst + oV, &mp.m[5], bar, s.z0, s.x0, o);
+                unsigned char *ax = dst + oX;
                 const int zs = s.z0 + ZS;
                 if (range_damped(s.x0, TX, p.ulo[0], p.uhi[0])) { tma_load_3d(ax, &mp.m[6], bar, zs, s.x0, o); ax += AUX; }
                 if (range_damped(o, 1, p.ulo[1], p.uhi[1])) { tma_load_3d(ax, &mp.m[7], bar, zs, s.x0, o); ax += AUX; }
@@ -374,10 +356,10 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             const S *Bu = reinterpret_cast<const S *>(sbp);
             const S *Bw = reinterpret_cast<const S *>(sbp + oW);
             const S *Bp = reinterpret_cast<const S *>(sbp + oP);
-            const float *Br = reinterpret_cast<const float *>(sbp + oR);  // K, or rho (damped items)
+            const float *Br = reinterpret_cast<const float *>(sbp + oR);
             const float *Bvp = reinterpret_cast<const float *>(sbp + oV);
             // split tiles as packed by the producer: x, then y, then z, present ones only
-            const S *Bx = reinterpret_cast<const S *>(sbp + oV + L::PAR2);
+            const S *Bx = reinterpret_cast<const S *>(sbp + oX);
             const S *By = Bx + (tdx ? L::C : 0u);
             const S *Bz = By + ((o < p.ulo[1] || o >= p.uhi[1]) ? L::C : 0u);
             // u at tile rows xw .. xw+R+6 of this lane's z pair: us[j] = u(x = xw - 4 + j)
@@ -409,28 +391,19 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 xx = T2{xa, xb};
                 zz = T2{za, zb};
             };
-            // (((1 * rho) * vp) * vp) == (rho * vp) * vp: on items off every damped axis
-            // the precomputed K, otherwise formed here (..iso..:182-184)
-            const bool pd = !L::KP || tdx || dym || tdz;
-            auto rvv = [&](int bi) -> T2 {
-                if (!pd) {
-                    const float2 k2 = *reinterpret_cast<const float2 *>(Br + bi);
-                    return T2{(T)k2.x, (T)k2.y};
-                }
-                const float2 rv = *reinterpret_cast<const float2 *>(Br + bi);
-                const float2 vv = *reinterpret_cast<const float2 *>(Bvp + bi);
-                return T2{((T)rv.x * (T)vv.x) * (T)vv.x, ((T)rv.y * (T)vv.y) * (T)vv.y};
-            };
             if (fast && !dym) {  // undamped interior tile and plane: P - gx - gy - gz, a1 == 1
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     const int bi = (xw + r) * 32 + zl;
                     T2 xx, zz;
                     deriv(r, xx, zz);
+                    const float2 rv = *reinterpret_cast<const float2 *>(Br + bi);
+                    const float2 vv = *reinterpret_cast<const float2 *>(Bvp + bi);
                     const T2 Po = ld2<T>(Bp, bi);
-                    const T2 t = rvv(bi);
-                    const T pa = ((Po.a - (t.a * dtx) * xx.a) - (t.a * dty) * yy[r].a) - (t.a * dtz) * zz.a;
-                    const T pb = ((Po.b - (t.b * dtx) * xx.b) - (t.b * dty) * yy[r].b) - (t.b * dtz) * zz.b;
+                    // (((1 * rho) * vp) * vp) == (rho * vp) * vp  (..iso..:182-184)
+                    const T ta = ((T)rv.x * (T)vv.x) * (T)vv.x, tb = ((T)rv.y * (T)vv.y) * (T)vv.y;
+                    const T pa = ((Po.a - (ta * dtx) * xx.a) - (ta * dty) * yy[r].a) - (ta * dtz) * zz.a;
+                    const T pb = ((Po.b - (tb * dtx) * xx.b) - (tb * dty) * yy[r].b) - (tb * dtz) * zz.b;
                     st2<S, T>(P, gb[r] + po, pa, pb);
                 }
                 return;
@@ -441,16 +414,11 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             // keeps its split component, an undamped one subtracts its term directly; the
             // selects keep the operation order, so undamped cells get ((P - gx) - gy) - gz.
             // a1 == 1 off the PML, so one product chain serves every cell (..iso..:182-184).
-            // rv, vv: rho and vp on items that touch a damped axis; elsewhere every a1 is
-            // 1, rv holds K and the products reduce to it
             auto upd = [&](T Po, T xx, T yy_, T zz, float rv, float vv, bool dx, bool dz, float ax1_, float ax2_,
                            float az1_, float az2_, T cx, T cy, T cz, T &nx, T &ny, T &nz) -> T {
-                const T kx = pd ? ((((T)ax1_ * (T)rv) * (T)vv) * (T)vv) : (T)rv;
-                const T ky = pd ? ((((T)ay1 * (T)rv) * (T)vv) * (T)vv) : (T)rv;
-                const T kz = pd ? ((((T)az1_ * (T)rv) * (T)vv) * (T)vv) : (T)rv;
-                const T gx = (kx * dtx) * xx;
-                const T gy = (ky * dty) * yy_;
-                const T gz = (kz * dtz) * zz;
+                const T gx = (((((T)ax1_ * (T)rv) * (T)vv) * (T)vv) * dtx) * xx;
+                const T gy = (((((T)ay1 * (T)rv) * (T)vv) * (T)vv) * dty) * yy_;
+                const T gz = (((((T)az1_ * (T)rv) * (T)vv) * (T)vv) * dtz) * zz;
                 T q = Po;
                 q = dx ? q - cx : q;
                 q = dym ? q - cy : q;
@@ -472,7 +440,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 T2 xx, zz;
                 deriv(r, xx, zz);
                 const float2 rv = *reinterpret_cast<const float2 *>(Br + bi);
-                const float2 vv = pd ? *reinterpret_cast<const float2 *>(Bvp + bi) : float2{0.0f, 0.0f};
+                const float2 vv = *reinterpret_cast<const float2 *>(Bvp + bi);
                 const T2 Po = ld2<T>(Bp, bi);
                 // split components present in this item (tile- and plane-level flags)
                 const T2 cx = tdx ? ld2<T>(Bx, bi) : T2{0, 0};
@@ -520,8 +488,8 @@ static cudaError_t launch_iso_t(const K1Launch &L, cudaStream_t st) {
                          (S *)L.out0, (S *)L.out1, (S *)L.out2, p);
     }
     static SmemAttr attr;
-    Maps<10> mp;
-    for (int i = 0; i < 10; ++i) mp.m[i] = L.maps[i];
+    Maps<9> mp;
+    for (int i = 0; i < 9; ++i) mp.m[i] = L.maps[i];
     auto kern = iso_stress<TX, S, D, R>;
     const int grid = k1_sweep<TX>(p, kern, NT, IsoStrL<TX, S, D>::TOTAL, L.grid, L.mode, L.rot);
     return k1_launch(kern, NT, IsoStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, p);
