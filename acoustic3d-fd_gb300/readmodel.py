@@ -298,32 +298,70 @@ class FD:
         jt = int(np.float32(self.sg.receiver_dt) / np.float32(self.dt))
         np.ascontiguousarray(rec[::jy, ::jx, ::jt], dtype=np.float32).tofile(shotname)
 
-    def _survey_worker(self, tasks, device, graph):
+    def _survey_worker(self, tasks, device, graph, batch=0, chunk=4):
+        """Runs the tasks on one device, `chunk` shots per a3d_run_batch call (the
+        multi-shot batch size for VTI when batch > 1); a writer thread writes each
+        call's record files while the next call runs on the GPU (the call releases
+        the interpreter lock), so file output overlaps compute and the host holds
+        at most two calls' records."""
+        import queue
+        import threading
         import a3d
         if not tasks:
             return 0
-        recs, _ = a3d.run_batch(self.engine_config(), self.read_models(), [tuple(t[:3]) for t in tasks],
-                                graph=graph, device=device)
-        for t, rec in zip(tasks, recs):
-            self.write_record(self.shot_name(t), rec)
+        cfg = self.engine_config()
+        cfg.batch = batch if (batch > 1 and self.physics == "vti") else 0
+        models = self.read_models()
+        step = max(cfg.batch, chunk, 1)
+        q = queue.Queue(maxsize=1)
+        failed = []
+
+        def writer():
+            while True:
+                item = q.get()
+                if item is None:
+                    return
+                if failed:
+                    continue
+                try:
+                    for t, rec in item:
+                        self.write_record(self.shot_name(t), rec)
+                except Exception as exc:  # reported after the GPU work stops
+                    failed.append(exc)
+
+        th = threading.Thread(target=writer, daemon=True)
+        th.start()
+        try:
+            for i in range(0, len(tasks), step):
+                part = tasks[i:i + step]
+                recs, _ = a3d.run_batch(cfg, models, [tuple(t[:3]) for t in part], graph=graph, device=device)
+                if failed:
+                    break
+                q.put(list(zip(part, recs)))
+        finally:
+            q.put(None)
+            th.join()
+        if failed:
+            raise failed[0]
         return len(tasks)
 
-    def survey(self, devices=(0,), skip_existing=False, graph=True):
+    def survey(self, devices=(0,), skip_existing=False, graph=True, batch=0):
         """Every shot of this node through the batched entry point: one worker process
         per device, each with its round-robin share of the shots (as allocateNode splits
-        nodes, readmodel.py:121-126) in one a3d_run_batch call, records written in the
-        legacy layout.  With skip_existing, complete record files are kept (resume).
-        Snapshots are not taken on this path (run() takes them)."""
+        nodes, readmodel.py:121-126) in a3d_run_batch calls, records written in the
+        legacy layout while the next shots run.  batch > 1 (VTI): shots advance that
+        many at a time in multi-shot sweeps.  With skip_existing, complete record files
+        are kept (resume).  Snapshots are not taken on this path (run() takes them)."""
         tasks = [t for t in self.sg.nodetask[self.nodei]
                  if not (skip_existing and os.path.exists(self.shot_name(t)) and
                          os.path.getsize(self.shot_name(t)) == self.record_bytes())]
         devices = list(devices)
         if len(devices) == 1:
-            return self._survey_worker(tasks, devices[0], graph)
+            return self._survey_worker(tasks, devices[0], graph, batch)
         from multiprocessing import get_context
         ctx = get_context("spawn")
         with ctx.Pool(len(devices)) as pool:
-            res = [pool.apply_async(self._survey_worker, (tasks[k::len(devices)], d, graph))
+            res = [pool.apply_async(self._survey_worker, (tasks[k::len(devices)], d, graph, batch))
                    for k, d in enumerate(devices)]
             return sum(r.get() for r in res)
 

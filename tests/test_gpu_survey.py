@@ -49,3 +49,16 @@ def test_survey_files_equal_legacy_files(engine_lib, tmp_path, eng):
     assert batched.survey(devices=(0,), skip_existing=True) == 1
     t = batched.sg.nodetask[0][1]
     assert open(batched.shot_name(t), "rb").read() == open(legacy.shot_name(t), "rb").read()
+
+
+def test_vti_survey_in_multishot_sweeps(engine_lib, tmp_path):
+    """batch=3 over the node's 4 shots: one sweep of 3 and one of 1, the record files
+    of both written while the other runs, byte for byte the legacy entry point's."""
+    import readmodel as R
+    legacy = _setup(R, "vti", tmp_path, "legacy")
+    for t in legacy.sg.nodetask[0]:
+        legacy.run(t, 0)
+    batched = _setup(R, "vti", tmp_path, "sweeps")
+    assert batched.survey(devices=(0,), batch=3) == 4
+    for t in legacy.sg.nodetask[0]:
+        assert open(batched.shot_name(t), "rb").read() == open(legacy.shot_name(t), "rb").read()
