@@ -175,9 +175,10 @@ void *a3d_engine::dfield(size_t es) {
     return p ? p + Grid::zoff * es : nullptr;
 }
 
-void *a3d_engine::dfield_batch() {
-    char *p = (char *)dalloc(fstride * esz * nbatch);
-    return p ? p + Grid::zoff * esz : nullptr;
+void *a3d_engine::dfield_batch(bool pressure) {
+    const size_t es = fsize(pressure);
+    char *p = (char *)dalloc((pressure ? fstride_p : fstride) * es * nbatch);
+    return p ? p + Grid::zoff * es : nullptr;
 }
 
 // edge-replicated padding of a model on the device: the reference's three one-axis
@@ -253,10 +254,10 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     float *raw = nullptr;  // device scratch for one model array
     CUDA_TRY(cudaMalloc(&raw, (size_t)c.nx * c.ny * c.nz * 4));
     struct FreeRaw { float *p; ~FreeRaw() { cudaFree(p); } } free_raw{raw};
-    const size_t fb = e->nbatch > 1 ? e->fstride * e->esz * e->nbatch : g.elems() * e->esz;
-    auto field = [&](void **p) -> int {
-        *p = e->nbatch > 1 ? e->dfield_batch() : e->dfield(e->esz);
-        return *p ? A3D_OK : fail(A3D_E_NOMEM, "device allocation of %zu bytes failed", fb);
+    // u, v, w (pressure = false) and P, Q, split components (pressure = true)
+    auto field = [&](void **p, bool pressure = false) -> int {
+        *p = e->nbatch > 1 ? e->dfield_batch(pressure) : e->dfield(e->fsize(pressure));
+        return *p ? A3D_OK : fail(A3D_E_NOMEM, "device allocation of a %dx%dx%d field failed", g.nnz, g.nnx, g.nny);
     };
     int rc;
     e->rec = (float *)e->dalloc((size_t)c.nt * c.nx * c.ny * 4 * e->nbatch);
@@ -328,13 +329,14 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     // mute velocity: the padded model's element 1, i.e. model cell (0,0,0) (..iso..:340)
     e->v_mute = vel[0];
     if (c.physics != A3D_ISO) e->v_mute = vel[0] * sqrtf(1.0f + 2.0f * eps[0]);  // ..vti..:357
-    if ((rc = field(&e->u)) || (rc = field(&e->v)) || (rc = field(&e->w)) || (rc = field(&e->P)) ||
-        (rc = field(&e->px)) || (rc = field(&e->py)) || (rc = field(&e->pz)))
+    if ((rc = field(&e->u)) || (rc = field(&e->v)) || (rc = field(&e->w)) || (rc = field(&e->P, true)) ||
+        (rc = field(&e->px, true)) || (rc = field(&e->py, true)) || (rc = field(&e->pz, true)))
         return rc;
     if (e->fused_ok && ((rc = field(&e->u2)) || (rc = field(&e->v2)) || (rc = field(&e->w2)) || (rc = field(&e->P2))))
         return rc;
     if (c.physics != A3D_ISO) {
-        if ((rc = field(&e->Q)) || (rc = field(&e->qx)) || (rc = field(&e->qy)) || (rc = field(&e->qz)))
+        if ((rc = field(&e->Q, true)) || (rc = field(&e->qx, true)) || (rc = field(&e->qy, true)) ||
+            (rc = field(&e->qz, true)))
             return rc;
     }
     // PML profiles (..iso..:193-195 and 263-291): d0 from the padded model's middle element
@@ -417,6 +419,7 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
         const double dmin = std::min(c.dx, std::min(c.dy, c.dz));
         if (amax > 0.0f) e->sig_p = std::ldexp(1.0f, (int)std::floor(std::log2(2048.0 / amax)));
         e->sig_v = e->sig_p * std::ldexp(1.0f, (int)std::lround(std::log2(dmin * rmean / c.dt)));
+        if (e->pfloat) e->sig_p = 1.0f;  // float pressures: unscaled; u, v, w keep their range
     }
     // tensor maps for both tile widths
     const bool f64 = e->fp64;
@@ -424,11 +427,16 @@ static int engine_setup(a3d_engine *e, const float *vel, const float *rho, const
     const int tx = t ? 16 : 8;
     CUtensorMap *mvel = e->mvel[t], *mstr = e->mstr[t];
     int b0, b1;
+    // pressure fields (P, Q, split components) are float under A3D_FP16V
     auto mk = [&](CUtensorMap *m, const void *p, bool isfield, int box) {
-        box_dims(box, tx, b0, b1, isfield && e->half ? 48 : 40);
+        const bool pf = isfield && e->pfloat && (p == e->P || p == e->Q || p == e->px || p == e->py ||
+                                                 p == e->pz || p == e->qx || p == e->qy || p == e->qz);
+        const int dt = isfield ? (f64 ? 3 : (pf ? 0 : e->half)) : 0;
+        box_dims(box, tx, b0, b1, dt == 1 || dt == 2 ? 48 : 40);
         if (isfield && e->nbatch > 1)  // every shot's copy of a wavefield: 4-D map
-            return make_map(m, p, f64 ? 3 : e->half, g, b0, b1, e->nbatch, e->fstride * e->esz);
-        return make_map(m, p, isfield ? (f64 ? 3 : e->half) : 0, g, b0, b1);
+            return make_map(m, p, dt, g, b0, b1, e->nbatch,
+                            pf ? e->fstride_p * e->esz_p : e->fstride * e->esz);
+        return make_map(m, p, dt, g, b0, b1);
     };
     if (c.physics == A3D_ISO) {
         e->nvel = 5;
@@ -688,6 +696,7 @@ int a3d_engine::autotune_form() {
         L.out0 = kk == 0 ? u : P; L.out1 = kk == 0 ? v : Q; L.out2 = w;
         L.tx = tc.tx; L.depth = tc.depth; L.mode = tc.mode; L.rows = tc.rows; L.fp64 = fp64;
         L.half = half;
+        L.pf = pfloat;
         L.rot = tc.rot;
         if (nbatch > 1) {  // multi-shot kernels over every copy (no source: d_shots lie outside)
             L.ms = 1;
@@ -695,6 +704,7 @@ int a3d_engine::autotune_form() {
             L.sblk = tc.sblk;
             p.shots = d_shots;
             p.fstride = fstride;
+            p.fstride_p = fstride_p;
             p.rstride = (size_t)c.nt * c.nx * c.ny;
         }
         p.svp = p.spv = p.rec_scale = 1.0f;
@@ -903,7 +913,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
             crop_window<double><<<1024, 256, 0, st>>>((const double *)field, dst, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
         else if (half == 1)
             crop_window<__nv_bfloat16><<<1024, 256, 0, st>>>((const __nv_bfloat16 *)field, dst, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
-        else if (half == 2)
+        else if (half == 2 && !pfloat)  // A3D_FP16V snapshots P, stored as float
             crop_window<__half><<<1024, 256, 0, st>>>((const __half *)field, dst, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
         else
             crop_window<float><<<1024, 256, 0, st>>>((const float *)field, dst, c.nx, c.ny, c.nz, pad, g.ldz, g.nnx, sc);
@@ -978,8 +988,10 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         if (rc) return rc;
     } else {
         void *fields[15] = {u, v, w, P, Q, px, py, pz, qx, qy, qz, u2, v2, w2, P2};
-        for (void *f : fields)
-            if (f) CUDA_TRY(cudaMemsetAsync(field_alloc(f, esz), 0, fb, st));
+        for (int k = 0; k < 15; ++k) {
+            const bool pr = k >= 3 && k < 11;  // P, Q and split components
+            if (fields[k]) CUDA_TRY(cudaMemsetAsync(field_alloc(fields[k], fsize(pr)), 0, g.elems() * fsize(pr), st));
+        }
         const int np = npml;
         K1Launch Lv{}, Ls{};
         K1Params p{};
@@ -1011,6 +1023,7 @@ int a3d_engine::run(const a3d_shot &s, float *rec_dev, const SnapHook *hook, dou
         Ls.tx = tune[1].tx; Ls.depth = tune[1].depth; Ls.mode = tune[1].mode; Ls.rows = tune[1].rows;
         Lv.rot = tune[0].rot; Ls.rot = tune[1].rot;
         Lv.fp64 = Ls.fp64 = fp64; Lv.half = Ls.half = half; Lv.grid = Ls.grid = 0;
+        Lv.pf = Ls.pf = pfloat;
         auto launch = c.physics == A3D_ISO ? launch_iso : (c.physics == A3D_VTI ? launch_vti : launch_tti);
         if (learned && !cl_packed) return fail(A3D_E_ARG, "learned rim without a closure (a3d_engine_set_closure)");
         std::vector<int> tap_slot(tap_out ? c.nt : 0, -1);
@@ -1141,9 +1154,10 @@ int a3d_engine::run_shots(const a3d_shot *shots, int k, double *ms) {
                         mute_nt(ix, iy, shots[j].sx, shots[j].sy, shots[j].sz, c.dx, c.dy, c.dz, c.dt, c.fm, v_mute);
         CUDA_TRY(cudaMemcpyAsync(d_mute, mute.data(), mute.size() * 4, cudaMemcpyHostToDevice, st));
     }
-    const size_t fb = fstride * esz * (size_t)k;
-    for (void *f : {u, v, w, P, Q, px, py, pz, qx, qy, qz})
-        if (f) CUDA_TRY(cudaMemsetAsync(field_alloc(f, esz), 0, fb, st));
+    for (void *f : {u, v, w})
+        if (f) CUDA_TRY(cudaMemsetAsync(field_alloc(f, esz), 0, fstride * esz * (size_t)k, st));
+    for (void *f : {P, Q, px, py, pz, qx, qy, qz})
+        if (f) CUDA_TRY(cudaMemsetAsync(field_alloc(f, esz_p), 0, fstride_p * esz_p * (size_t)k, st));
     K1Launch Lv{}, Ls{};
     K1Params p{};
     p.nnz = g.nnz; p.nnx = g.nnx; p.nny = g.nny; p.ldz = g.ldz;
@@ -1156,6 +1170,7 @@ int a3d_engine::run_shots(const a3d_shot *shots, int k, double *ms) {
     p.s_x = p.s_y = p.s_z = -100;  // per shot: p.shots
     p.shots = d_shots;
     p.fstride = fstride;
+    p.fstride_p = fstride_p;
     p.rstride = (size_t)c.nt * c.nx * c.ny;
     p.taper = taper;
     p.px = px; p.py = py; p.pz = pz; p.qx = qx; p.qy = qy; p.qz = qz;
@@ -1176,6 +1191,7 @@ int a3d_engine::run_shots(const a3d_shot *shots, int k, double *ms) {
     Ls.tx = tune[1].tx; Ls.depth = tune[1].depth; Ls.mode = tune[1].mode; Ls.rows = tune[1].rows;
     Lv.rot = tune[0].rot; Ls.rot = tune[1].rot;
     Lv.fp64 = Ls.fp64 = false; Lv.half = Ls.half = half; Lv.grid = Ls.grid = 0;
+    Lv.pf = Ls.pf = pfloat;
     Lv.ms = Ls.ms = 1;
     Lv.nshot = Ls.nshot = k;
     Lv.sblk = tune[0].sblk;
@@ -1226,7 +1242,8 @@ static int validate(const a3d_config *c) {
     if (!(c->dx > 0) || !(c->dy > 0) || !(c->dz > 0) || !(c->dt > 0) || !(c->fm > 0))
         return fail(A3D_E_ARG, "dx, dy, dz, dt and fm must be positive");
     if (c->storage != A3D_FP32 && c->storage != A3D_FP64 &&
-        !((c->storage == A3D_BF16 || c->storage == A3D_FP16) && c->physics != A3D_2ORDER))
+        !((c->storage == A3D_BF16 || c->storage == A3D_FP16) && c->physics != A3D_2ORDER) &&
+        !(c->storage == A3D_FP16V && c->physics == A3D_VTI))
         return fail(A3D_E_UNSUPPORTED, "storage type %d is not built for this engine", c->storage);
     if (c->physics == A3D_ISO && (c->wtype < 1 || c->wtype > 6))
         return fail(A3D_E_ARG, "wavelet type %d outside 1..6", c->wtype);
@@ -1262,8 +1279,10 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
     e->cfg = *cfg;
     e->device = device;
     e->fp64 = cfg->storage == A3D_FP64;
-    e->half = cfg->storage == A3D_BF16 ? 1 : (cfg->storage == A3D_FP16 ? 2 : 0);
+    e->half = cfg->storage == A3D_BF16 ? 1 : ((cfg->storage == A3D_FP16 || cfg->storage == A3D_FP16V) ? 2 : 0);
+    e->pfloat = cfg->storage == A3D_FP16V;
     e->esz = e->fp64 ? 8 : (e->half ? 2 : 4);
+    e->esz_p = e->pfloat ? 4 : e->esz;
     e->tx = 8;
     e->nbatch = cfg->batch > 1 ? cfg->batch : 1;
     if (ph == A3D_2ORDER) {
@@ -1294,6 +1313,7 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
     }
     // one copy of a wavefield per shot of a multi-shot sweep, 256-byte aligned
     e->fstride = (e->g.elems() * e->esz + 255) / 256 * 256 / e->esz;
+    e->fstride_p = (e->g.elems() * e->esz_p + 255) / 256 * 256 / e->esz_p;
     if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) {
         delete e;

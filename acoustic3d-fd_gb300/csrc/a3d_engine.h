@@ -51,7 +51,10 @@ struct a3d_engine {
     // component holds K copies fstride elements apart (4-D tensor maps over them),
     // K records and K mute tables follow each other, d_shots the shots' source cells
     int nbatch = 1;
-    size_t fstride = 0;
+    size_t fstride = 0, fstride_p = 0;  // u, v, w / P, Q and split components (elements)
+    // A3D_FP16V: u, v, w float16 (half = 2, esz = 2), P, Q and split components float
+    bool pfloat = false;
+    size_t esz_p = 4;      // bytes per element of P, Q and the split components
     int4 *d_shots = nullptr;
     // power-of-two storage scales of 2-byte wavefields: sig_v for u, v, w, sig_p for P
     // and its split components (1 otherwise)
@@ -147,8 +150,10 @@ struct a3d_engine {
     ~a3d_engine();
     void *dalloc(size_t bytes);  // zeroed; null on failure
     void *dfield(size_t esz);    // zeroed padded field; returns its base (allocation + zoff)
-    // nbatch copies of a wavefield, fstride elements apart; returns the first copy's base
-    void *dfield_batch();
+    // nbatch copies of a wavefield (pressure: P, Q or a split component), fstride /
+    // fstride_p elements apart; returns the first copy's base
+    void *dfield_batch(bool pressure);
+    size_t fsize(bool pressure) const { return pressure ? esz_p : esz; }
     size_t field_bytes(size_t esz) const { return g.elems() * esz; }
     void *field_alloc(void *base, size_t es) const { return (char *)base - a3d::Grid::zoff * es; }
     int run(const a3d_shot &s, float *rec_dev, const a3d::SnapHook *hook, double *ms);

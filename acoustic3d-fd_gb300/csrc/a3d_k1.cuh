@@ -38,6 +38,7 @@ struct K1Params {
     // apart and their mute tables nx * ny ints apart
     const int4 *shots;
     size_t fstride, rstride;
+    size_t fstride_p;  // the same for P, Q and the split components (elements of their type)
 };
 
 enum K1Kind { K1_ISO_VEL = 0, K1_ISO_STR, K1_VTI_VEL, K1_VTI_STR, K1_TTI_VEL, K1_TTI_STR, K1_ISO_STEP };
@@ -62,6 +63,7 @@ struct K1Launch {
     int ms;     // 1: multi-shot kernels (VTI: 4-D wavefield maps, p.shots, p.fstride, p.rstride)
     int nshot;  // multi-shot kernels: shots this launch advances (1 .. the maps' shot count)
     int sblk;   // multi-shot kernels: grid tiles per block of the tile order (Sweep::sblk)
+    int pf;     // VTI with half == 2: P, Q and split components stored as float (A3D_FP16V)
 };
 
 cudaError_t launch_k1(const K1Launch &L, cudaStream_t st);
@@ -73,5 +75,6 @@ cudaError_t launch_iso(const K1Launch &L, cudaStream_t st);
 cudaError_t launch_iso_step(const K1Launch &L, cudaStream_t st);  // fused isotropic step (FP32)
 cudaError_t launch_vti(const K1Launch &L, cudaStream_t st);
 cudaError_t launch_vti_ms(const K1Launch &L, cudaStream_t st);  // L.ms (launch_vti forwards)
+cudaError_t launch_vti_pf(const K1Launch &L, cudaStream_t st);  // L.pf (launch_vti forwards)
 cudaError_t launch_tti(const K1Launch &L, cudaStream_t st);
 }  // namespace a3d

@@ -20,6 +20,7 @@ static cudaError_t launch_vti_half(const K1Launch &L, cudaStream_t st) {
 }
 
 cudaError_t launch_vti(const K1Launch &L, cudaStream_t st) {
+    if (L.pf) return launch_vti_pf(L, st);
     if (L.ms) return launch_vti_ms(L, st);
     if (L.fp64) return launch_vti_t<8, double, 0, 2>(L, st);
     if (L.half == 1) return launch_vti_half<__nv_bfloat16>(L, st);

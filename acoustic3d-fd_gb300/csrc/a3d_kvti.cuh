@@ -10,19 +10,21 @@
 //               split components only on damped PML axes, record + mute fused.
 #pragma once
 #include <climits>
+#include <type_traits>
 
 #include "a3d_k1dev.cuh"
 
 namespace a3d {
 
 // ===========================================================================
-// vti_vel: maps {P (HX), Q (HZ), u, v, w (core), 1/rho (core float)}
-template <int TX, class S, int D>
+// vti_vel: maps {P (HX), Q (HZ), u, v, w (core), 1/rho (core float)}; S stores u, v,
+// w and SP stores P, Q (the same type, or float with 2-byte velocities)
+template <int TX, class S, int D, class SP = S>
 struct VtiVelL {
-    static constexpr int QW = ZHalo<S>::W;  // Q tile rows: z halo ZH
+    static constexpr int QW = ZHalo<SP>::W;  // Q tile rows: z halo ZH
     static constexpr uint32_t C = 32 * TX, PX = 32 * (TX + 8), QZ = QW * TX;
-    static constexpr uint32_t A_BYTES = PX * sizeof(S);
-    static constexpr uint32_t B_BYTES = (QZ + 3 * C) * sizeof(S) + C * 4;
+    static constexpr uint32_t A_BYTES = PX * sizeof(SP);
+    static constexpr uint32_t B_BYTES = QZ * sizeof(SP) + 3 * C * sizeof(S) + C * 4;
     static constexpr size_t A_STRIDE = (A_BYTES + 127) / 128 * 128;
     static constexpr size_t B_STRIDE = (B_BYTES + 127) / 128 * 128;
     using RG = Ring<D, A_STRIDE, B_STRIDE>;
@@ -31,15 +33,17 @@ struct VtiVelL {
     static constexpr size_t RB = RG::RB, B_OFF = RG::B_OFF, BAR_OFF = RG::BAR_OFF, TOTAL = RG::TOTAL;
 };
 
-template <int TX, class S, int D, int R, bool MS>
+template <int TX, class S, int D, int R, bool MS, bool PF>
 __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     vti_vel(const __grid_constant__ Maps<6> mp, S *__restrict__ u, S *__restrict__ v,
             S *__restrict__ w, const __grid_constant__ K1Params p) {
-    using L = VtiVelL<TX, S, D>;
+    using SP = std::conditional_t<PF, float, S>;  // P, Q storage
+    using L = VtiVelL<TX, S, D, SP>;
     using T = typename Arith<S>::T;
     using T2 = Two<T>;
     constexpr int NW = TX / (2 * R), NC = 32 * NW, QW = L::QW;
-    constexpr int ZS = WFieldZShift<S>::v, ZH = ZHalo<S>::ZH;
+    constexpr int ZS = WFieldZShift<S>::v;                          // u, v, w maps
+    constexpr int ZSP = WFieldZShift<SP>::v, ZH = ZHalo<SP>::ZH;    // P, Q maps
     static_assert(NW >= 1, "a warp covers 2R tile rows");
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<typename L::Bars *>(smem + L::BAR_OFF);
@@ -50,7 +54,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     cta_range(p.sw, w0, w1);
     if (w0 >= w1) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr size_t oU = L::QZ * sizeof(S), oV = oU + L::C * sizeof(S), oW = oV + L::C * sizeof(S),
+    constexpr size_t oU = L::QZ * sizeof(SP), oV = oU + L::C * sizeof(S), oW = oV + L::C * sizeof(S),
                      oR = oW + L::C * sizeof(S);
 
     if (warp == NW) {  // producer warp: one thread issues every copy
@@ -60,10 +64,10 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             p.sw, w0, w1, bars, ringB, p.err, [](const Seg &, int) { return (uint32_t)L::B_STRIDE; },
             [&](uint32_t sa, unsigned char *dst, uint32_t, uint64_t *bar, const Seg &s, int q) {
                 mbar_arrive_expect_tx(bar, L::A_BYTES + (dst ? L::B_BYTES : 0u));
-                tma_field<MS>(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0 + ZS, s.x0 - MM, q, s.shot);
+                tma_field<MS>(ringA + sa * L::A_STRIDE, &mp.m[0], bar, s.z0 + ZSP, s.x0 - MM, q, s.shot);
                 if (!dst) return;
                 const int o = q - MM;
-                tma_field<MS>(dst, &mp.m[1], bar, s.z0 - ZH + ZS, s.x0, o, s.shot);
+                tma_field<MS>(dst, &mp.m[1], bar, s.z0 - ZH + ZSP, s.x0, o, s.shot);
                 tma_field<MS>(dst + oU, &mp.m[2], bar, s.z0 + ZS, s.x0, o, s.shot);
                 tma_field<MS>(dst + oV, &mp.m[3], bar, s.z0 + ZS, s.x0, o, s.shot);
                 tma_field<MS>(dst + oW, &mp.m[4], bar, s.z0 + ZS, s.x0, o, s.shot);
@@ -119,11 +123,11 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
         },
         [&](auto ph, uint32_t sa, const Seg &s, int q) {
             constexpr int P_ = decltype(ph)::value;
-            S *A = reinterpret_cast<S *>(ringA + sa * L::A_STRIDE);
+            SP *A = reinterpret_cast<SP *>(ringA + sa * L::A_STRIDE);
             if (q == srcP) {
                 if (threadIdx.x == 0) {
                     const int at = (sc.x - (s.x0 - MM)) * 32 + (sc.z - s.z0);
-                    A[at] = to_store<S, T>(ld<T>(A, at) + (T)p.amp0);
+                    A[at] = to_store<SP, T>(ld<T>(A, at) + (T)p.amp0);
                     fence_proxy_async();
                 }
                 consumer_sync(NC);
@@ -132,19 +136,19 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             for (int r = 0; r < R; ++r) win[r][P_] = ld2<T>(A, c0 + r * 32);
         },
         [&](int ph, uint32_t sa, uint32_t sh, const unsigned char *sbc, const Seg &s, int q) {
-            S *A = reinterpret_cast<S *>(ringA + sa * L::A_STRIDE);
+            SP *A = reinterpret_cast<SP *>(ringA + sa * L::A_STRIDE);
             unsigned char *sbp = const_cast<unsigned char *>(sbc);
             const int o = q - MM;
             if (q == srcP || o == srcQ) {  // one plane per shot and tile: patch, then publish
                 if (threadIdx.x == 0) {
                     if (q == srcP) {
                         const int at = (sc.x - (s.x0 - MM)) * 32 + (sc.z - s.z0);
-                        A[at] = to_store<S, T>(ld<T>(A, at) + (T)p.amp0);
+                        A[at] = to_store<SP, T>(ld<T>(A, at) + (T)p.amp0);
                     }
                     if (o == srcQ) {
-                        S *Bq = reinterpret_cast<S *>(sbp);
+                        SP *Bq = reinterpret_cast<SP *>(sbp);
                         const int at = (sc.x - s.x0) * QW + (sc.z - (s.z0 - ZH));
-                        Bq[at] = to_store<S, T>(ld<T>(Bq, at) + (T)p.amp1);
+                        Bq[at] = to_store<SP, T>(ld<T>(Bq, at) + (T)p.amp1);
                     }
                     fence_proxy_async();
                 }
@@ -166,8 +170,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                     yy[r] = T2{a, b};
                 }
             });
-            const S *Ao = reinterpret_cast<const S *>(ringA + sh * L::A_STRIDE);
-            const S *Bq = reinterpret_cast<const S *>(sbp);
+            const SP *Ao = reinterpret_cast<const SP *>(ringA + sh * L::A_STRIDE);
+            const SP *Bq = reinterpret_cast<const SP *>(sbp);
             const S *Bu = reinterpret_cast<const S *>(sbp + oU);
             const S *Bv = reinterpret_cast<const S *>(sbp + oV);
             const S *Bw = reinterpret_cast<const S *>(sbp + oW);
@@ -220,14 +224,14 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
 // ===========================================================================
 // vti_stress: maps {v (core), u (HX), w (HZ), P, Q (core), rho, vp, eps, del (core float),
 //                   px, py, pz, qx, qy, qz (core; only for tiles/planes on a damped axis)}
-template <int TX, class S, int D>
+template <int TX, class S, int D, class SP = S>
 struct VtiStrL {
     static constexpr uint32_t C = 32 * TX, UX = 32 * (TX + 8), WZ = ZHalo<S>::W * TX;
     static constexpr uint32_t A_BYTES = C * sizeof(S);
     // fixed part of a B item (u, w, P, Q, rho, vp, eps, del), then the (p, q) split
-    // pair of each damped axis, in x, y, z order
-    static constexpr uint32_t B_FIXED = (UX + WZ + 2 * C) * sizeof(S) + 4 * C * 4;
-    static constexpr uint32_t AUX = C * sizeof(S);
+    // pair of each damped axis, in x, y, z order; S stores u, v, w, SP P, Q and splits
+    static constexpr uint32_t B_FIXED = (UX + WZ) * sizeof(S) + 2 * C * sizeof(SP) + 4 * C * 4;
+    static constexpr uint32_t AUX = C * sizeof(SP);
     static constexpr uint32_t B_BYTES = B_FIXED + 6 * AUX;
     static constexpr size_t A_STRIDE = (A_BYTES + 127) / 128 * 128;
     static constexpr size_t B_STRIDE = (B_BYTES + 127) / 128 * 128;
@@ -294,15 +298,17 @@ __device__ __forceinline__ void vti_cell(T Po, T Qo, T xx, T yy, T zz, float rv,
     Qn = qq;
 }
 
-template <int TX, class S, int D, int R, bool MS>
+template <int TX, class S, int D, int R, bool MS, bool PF>
 __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
-    vti_stress(const __grid_constant__ Maps<15> mp, S *__restrict__ P, S *__restrict__ Q,
-               const __grid_constant__ K1Params p) {
-    using L = VtiStrL<TX, S, D>;
+    vti_stress(const __grid_constant__ Maps<15> mp, std::conditional_t<PF, float, S> *__restrict__ P,
+               std::conditional_t<PF, float, S> *__restrict__ Q, const __grid_constant__ K1Params p) {
+    using SP = std::conditional_t<PF, float, S>;  // P, Q and split-component storage
+    using L = VtiStrL<TX, S, D, SP>;
     using T = typename Arith<S>::T;
     using T2 = Two<T>;
     constexpr int NW = TX / (2 * R);
-    constexpr int ZS = WFieldZShift<S>::v, ZH = ZHalo<S>::ZH, WW = ZHalo<S>::W;
+    constexpr int ZS = WFieldZShift<S>::v, ZH = ZHalo<S>::ZH, WW = ZHalo<S>::W;  // u, v, w maps
+    constexpr int ZSP = WFieldZShift<SP>::v;                                      // P, Q, split maps
     static_assert(NW >= 1, "a warp covers 2R tile rows");
     extern __shared__ __align__(128) unsigned char smem[];
     auto &bars = *reinterpret_cast<typename L::Bars *>(smem + L::BAR_OFF);
@@ -313,11 +319,11 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     cta_range(p.sw, w0, w1);
     if (w0 >= w1) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr size_t oW = L::UX * sizeof(S), oP = oW + L::WZ * sizeof(S), oQ = oP + L::C * sizeof(S),
-                     oF = oQ + L::C * sizeof(S),  // then rho, vp, eps, del floats
+    constexpr size_t oW = L::UX * sizeof(S), oP = oW + L::WZ * sizeof(S), oQ = oP + L::C * sizeof(SP),
+                     oF = oQ + L::C * sizeof(SP),  // then rho, vp, eps, del floats
                      oX = L::B_FIXED;             // split pairs of the damped axes follow
     constexpr uint32_t AUX = L::AUX;
-    S *px = (S *)p.px, *py = (S *)p.py, *pz = (S *)p.pz, *qx = (S *)p.qx, *qy = (S *)p.qy, *qz = (S *)p.qz;
+    SP *px = (SP *)p.px, *py = (SP *)p.py, *pz = (SP *)p.pz, *qx = (SP *)p.qx, *qy = (SP *)p.qy, *qz = (SP *)p.qz;
 
     if (warp == NW) {  // producer warp: one thread issues every copy
         if (lane != 0) return;
@@ -337,8 +343,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 const int o = q - MM;
                 tma_field<MS>(dst, &mp.m[1], bar, s.z0 + ZS, s.x0 - MM, o, s.shot);
                 tma_field<MS>(dst + oW, &mp.m[2], bar, s.z0 - ZH + ZS, s.x0, o, s.shot);
-                tma_field<MS>(dst + oP, &mp.m[3], bar, s.z0 + ZS, s.x0, o, s.shot);
-                tma_field<MS>(dst + oQ, &mp.m[4], bar, s.z0 + ZS, s.x0, o, s.shot);
+                tma_field<MS>(dst + oP, &mp.m[3], bar, s.z0 + ZSP, s.x0, o, s.shot);
+                tma_field<MS>(dst + oQ, &mp.m[4], bar, s.z0 + ZSP, s.x0, o, s.shot);
                 // rho, vp, eps, del: one copy for every shot
                 for (int k = 0; k < 4; ++k) tma_load_3d(dst + oF + k * L::C * 4, &mp.m[5 + k], bar, s.z0, s.x0, o);
                 unsigned char *ax = dst + oX;
@@ -346,8 +352,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                                     range_damped(s.z0, 32, p.ulo[2], p.uhi[2])};
                 for (int a = 0; a < 3; ++a)
                     if (dm[a]) {
-                        tma_field<MS>(ax, &mp.m[9 + a], bar, s.z0 + ZS, s.x0, o, s.shot);
-                        tma_field<MS>(ax + AUX, &mp.m[12 + a], bar, s.z0 + ZS, s.x0, o, s.shot);
+                        tma_field<MS>(ax, &mp.m[9 + a], bar, s.z0 + ZSP, s.x0, o, s.shot);
+                        tma_field<MS>(ax + AUX, &mp.m[12 + a], bar, s.z0 + ZSP, s.x0, o, s.shot);
                         ax += 2 * AUX;
                     }
             });
@@ -365,7 +371,7 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
     int zmin = 0;  // tile's first z (SV-ball distance test)
     int x0s = 0;
     int3 sc = make_int3(0, 0, 0);  // source cell of the segment's shot
-    S *Pk = P, *Qk = Q;            // the segment's shot's fields
+    SP *Pk = P, *Qk = Q;           // the segment's shot's fields
     float *reck = p.rec;
     const int *mutek = p.mute_nt;
     float ay1n = 1, ay2n = 1;
@@ -404,10 +410,10 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             x0s = s.x0;
             sc = shot_cell<MS>(p, s.shot);
             if constexpr (MS) {
-                const size_t fo = (size_t)s.shot * p.fstride;
+                const size_t fo = (size_t)s.shot * p.fstride_p;
                 Pk = P + fo; Qk = Q + fo;
-                px = (S *)p.px + fo; py = (S *)p.py + fo; pz = (S *)p.pz + fo;
-                qx = (S *)p.qx + fo; qy = (S *)p.qy + fo; qz = (S *)p.qz + fo;
+                px = (SP *)p.px + fo; py = (SP *)p.py + fo; pz = (SP *)p.pz + fo;
+                qx = (SP *)p.qx + fo; qy = (SP *)p.qy + fo; qz = (SP *)p.qz + fo;
                 reck = p.rec + (size_t)s.shot * p.rstride;
                 mutek = p.mute_nt ? p.mute_nt + (size_t)s.shot * p.nx * p.ny : nullptr;
             }
@@ -441,8 +447,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             });
             const S *Bu = reinterpret_cast<const S *>(sbp);
             const S *Bw = reinterpret_cast<const S *>(sbp + oW);
-            const S *Bp = reinterpret_cast<const S *>(sbp + oP);
-            const S *Bq = reinterpret_cast<const S *>(sbp + oQ);
+            const SP *Bp = reinterpret_cast<const SP *>(sbp + oP);
+            const SP *Bq = reinterpret_cast<const SP *>(sbp + oQ);
             const float *F = reinterpret_cast<const float *>(sbp + oF);
             T2 us[R + 7];
 #pragma unroll
@@ -458,9 +464,9 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
             const int ddz = max(0, max(zmin - sc.z, sc.z - (zmin + 31)));
             const bool ball = dy * dy + ddx * ddx + ddz * ddz <= 225;
             // split pairs as packed by the producer: x, then y, then z, present ones only
-            const S *Xp = reinterpret_cast<const S *>(sbp + oX);
-            const S *Yp = Xp + (tdx ? 2 * L::C : 0u);
-            const S *Zp = Yp + (dym ? 2 * L::C : 0u);
+            const SP *Xp = reinterpret_cast<const SP *>(sbp + oX);
+            const SP *Yp = Xp + (tdx ? 2 * L::C : 0u);
+            const SP *Zp = Yp + (dym ? 2 * L::C : 0u);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int bi = (xw + r) * 32 + zl, cw = (xw + r) * WW + (ZH - MM) + zl;
@@ -497,8 +503,8 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                                 1.f, 1.f, 1.f, 1.f, c0, c0, dtx, dty, dtz, pa, qa, n0, n1);
                     vti_cell<T>(Po.b, Qo.b, xb, yy[r].b, zb, rv.y, vv.y, eeb, ddb, false, false, false, 1.f, 1.f,
                                 1.f, 1.f, 1.f, 1.f, c0, c0, dtx, dty, dtz, pb, qb, n0, n1);
-                    st2<S, T>(Pk, g, pa, pb);
-                    st2<S, T>(Qk, g, qa, qb);
+                    st2<SP, T>(Pk, g, pa, pb);
+                    st2<SP, T>(Qk, g, qa, qb);
                     continue;
                 }
                 const T2 cpx = tdx ? ld2<T>(Xp, bi) : T2{0, 0}, cqx = tdx ? ld2<T>(Xp + L::C, bi) : T2{0, 0};
@@ -512,16 +518,16 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
                 vti_cell<T>(Po.b, Qo.b, xb, yy[r].b, zb, rv.y, vv.y, eeb, ddb, dxm[r], dym, dzb, ax1[r], ay1,
                             az1.y, ax2[r], ay2, az2.y, cpb, cqb, dtx, dty, dtz, pb, qb, npb, nqb);
                 if (act[r]) {
-                    st2m<S, T>(Pk, g, pa, pb, both);
-                    st2m<S, T>(Qk, g, qa, qb, both);
-                    if (dxm[r]) { st2m<S, T>(px, g, npa[0], npb[0], both); st2m<S, T>(qx, g, nqa[0], nqb[0], both); }
-                    if (dym) { st2m<S, T>(py, g, npa[1], npb[1], both); st2m<S, T>(qy, g, nqa[1], nqb[1], both); }
+                    st2m<SP, T>(Pk, g, pa, pb, both);
+                    st2m<SP, T>(Qk, g, qa, qb, both);
+                    if (dxm[r]) { st2m<SP, T>(px, g, npa[0], npb[0], both); st2m<SP, T>(qx, g, nqa[0], nqb[0], both); }
+                    if (dym) { st2m<SP, T>(py, g, npa[1], npb[1], both); st2m<SP, T>(qy, g, nqa[1], nqb[1], both); }
                     if (dza && dzb && both) {
-                        st2<S, T>(pz, g, npa[2], npb[2]);
-                        st2<S, T>(qz, g, nqa[2], nqb[2]);
+                        st2<SP, T>(pz, g, npa[2], npb[2]);
+                        st2<SP, T>(qz, g, nqa[2], nqb[2]);
                     } else {
-                        if (dza) { pz[g] = to_store<S, T>(npa[2]); qz[g] = to_store<S, T>(nqa[2]); }
-                        if (dzb && both) { pz[g + 1] = to_store<S, T>(npb[2]); qz[g + 1] = to_store<S, T>(nqb[2]); }
+                        if (dza) { pz[g] = to_store<SP, T>(npa[2]); qz[g] = to_store<SP, T>(nqa[2]); }
+                        if (dzb && both) { pz[g + 1] = to_store<SP, T>(npb[2]); qz[g + 1] = to_store<SP, T>(nqb[2]); }
                     }
                 }
                 if (o >= p.npml && o < p.npml + p.ny && (reca[r] | recb[r])) {  // ..vti..:313-323
@@ -534,8 +540,9 @@ __global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
         });
 }
 
-template <int TX, class S, int D, int R, bool MS>
+template <int TX, class S, int D, int R, bool MS, bool PF = false>
 static inline cudaError_t launch_vti_s(const K1Launch &L, cudaStream_t st) {
+    using SP = std::conditional_t<PF, float, S>;
     K1Params p = L.p;
     p.sw.nshot = MS ? (L.nshot > 1 ? L.nshot : 1) : 1;
     p.sw.sblk = MS ? L.sblk : 1;
@@ -544,17 +551,18 @@ static inline cudaError_t launch_vti_s(const K1Launch &L, cudaStream_t st) {
         static SmemAttr attr;
         Maps<6> mp;
         for (int i = 0; i < 6; ++i) mp.m[i] = L.maps[i];
-        auto kern = vti_vel<TX, S, D, R, MS>;
-        const int grid = k1_sweep<TX>(p, kern, NT, VtiVelL<TX, S, D>::TOTAL, L.grid, L.mode, L.rot);
-        return k1_launch(kern, NT, VtiVelL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0,
+        auto kern = vti_vel<TX, S, D, R, MS, PF>;
+        const int grid = k1_sweep<TX>(p, kern, NT, VtiVelL<TX, S, D, SP>::TOTAL, L.grid, L.mode, L.rot);
+        return k1_launch(kern, NT, VtiVelL<TX, S, D, SP>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0,
                          (S *)L.out1, (S *)L.out2, p);
     }
     static SmemAttr attr;
     Maps<15> mp;
     for (int i = 0; i < 15; ++i) mp.m[i] = L.maps[i];
-    auto kern = vti_stress<TX, S, D, R, MS>;
-    const int grid = k1_sweep<TX>(p, kern, NT, VtiStrL<TX, S, D>::TOTAL, L.grid, L.mode, L.rot);
-    return k1_launch(kern, NT, VtiStrL<TX, S, D>::TOTAL, p.sw.W, grid, st, attr, mp, (S *)L.out0, (S *)L.out1, p);
+    auto kern = vti_stress<TX, S, D, R, MS, PF>;
+    const int grid = k1_sweep<TX>(p, kern, NT, VtiStrL<TX, S, D, SP>::TOTAL, L.grid, L.mode, L.rot);
+    return k1_launch(kern, NT, VtiStrL<TX, S, D, SP>::TOTAL, p.sw.W, grid, st, attr, mp, (SP *)L.out0,
+                     (SP *)L.out1, p);
 }
 
 }  // namespace a3d

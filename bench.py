@@ -74,7 +74,13 @@ FUSED_BYTES = 44.0
 #   stress u, v, w, P, Q (2 B) + vp, eps, del + 4 trig read, P, Q written -> 42 B;
 #   step: (u, v, w, P, Q) read and written at 2 B + 5 float parameters -> 40 B
 STEP_BYTES_2B = {"iso": 24.0, "vti": 36.0, "tti": 40.0}
-STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2}
+# float16 u, v, w with float P, Q and split components (VTI, "fp16v"):
+#   velocity: P, Q (4 B) + u, v, w (2 B) + 1/rho read, u, v, w written -> 24 B; stress:
+#   u, v, w (2 B) + P, Q (4 B) + rho, vp, eps, del read, P, Q written -> 38 B; step
+#   (u, v, w) read and written at 2 B, (P, Q) at 4 B, 4 float parameters -> 44 B
+KERNEL_BYTES_MIXED = {"vti": (24.0, 38.0)}
+STEP_BYTES_MIXED = {"vti": 44.0}
+STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2, "fp16v": 4}
 
 
 def workload(name, nt_override=None):
@@ -530,14 +536,18 @@ def run_vti_batch(args):
     es = 4 if args.storage == "fp32" else 2
     # compulsory bytes per cell and shot: wavefields read and written per shot, the
     # model parameters once per tile for the whole sweep (1/rho in the velocity
-    # sweep; rho, vp, epsilon, delta in the stress sweep)
-    kb = (es * 8 + 4.0 / K, es * 7 + 16.0 / K)
+    # sweep; rho, vp, epsilon, delta in the stress sweep); velocity sweep: P, Q, u, v,
+    # w read, u, v, w written; stress sweep: u, v, w, P, Q read, P, Q written
+    ep = 4 if args.storage == "fp16v" else es  # bytes of P, Q
+    kb = (es * 6 + ep * 2 + 4.0 / K, es * 3 + ep * 4 + 16.0 / K)
     per = [kms[i] / kn[i] if kn[i] else 0.0 for i in range(2)]
     dom = 0 if per[0] >= per[1] else 1
     achieved = kb[dom] * cells * K / (per[dom] / 1000.0) / 1e9
     line = {"metric": "Gpts/s", "value": value, "unit": "Gpts/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if es == 4 else f"f32 arithmetic, {args.storage} wavefields",
+            "vs_baseline": None, "dtype": "f32" if es == 4 else (
+                "f32 arithmetic, f16 u, v, w, f32 P, Q" if args.storage == "fp16v" else
+                f"f32 arithmetic, {args.storage} wavefields"),
             "data": "synthetic",
             "config": dict(meta, workload="vti1order_%s_nt%d_sweep%d" % (meta["model"], nt, K),
                            shots=[list(x) for x in shots], batch=K, storage=args.storage, parallelism="replicas1",
@@ -647,6 +657,8 @@ def main():
     meta["storage"] = args.storage
     if args.storage != "fp32" and cfgd["physics"] not in ("iso", "vti", "tti"):
         raise SystemExit("2-byte storage is built for the 1st-order engines only")
+    if args.storage == "fp16v" and cfgd["physics"] != "vti":
+        raise SystemExit("fp16v storage is built for the VTI engine only")
     if args.impl == "reference":
         run_reference(args, cfgd, models, shot, meta)
         return
@@ -718,10 +730,11 @@ def main():
     # ---- roofline of the dominant kernel
     peak, peak_kind = measured_peak()
     two = args.storage != "fp32"
-    kb = (KERNEL_BYTES_2B if two else KERNEL_BYTES)[eng]
+    mixed = args.storage == "fp16v"
+    kb = (KERNEL_BYTES_MIXED if mixed else KERNEL_BYTES_2B if two else KERNEL_BYTES)[eng]
     if desc.get("fused"):  # one fused step per time step: u, v, w, P, 1/rho, rho, vp read, u, v, w, P written
         kb = (FUSED_BYTES, None)
-    step_b = (STEP_BYTES_2B if two else STEP_BYTES)[eng]
+    step_b = (STEP_BYTES_MIXED if mixed else STEP_BYTES_2B if two else STEP_BYTES)[eng]
     per = [kms[i] / kn[i] if kn[i] else 0.0 for i in range(2)]
     dom = 0 if (per[0] >= per[1] or kb[1] is None) else 1
     achieved = kb[dom] * cells / (per[dom] / 1000.0) / 1e9
@@ -807,7 +820,9 @@ def main():
         clocks = clk.summary()
         line = {"metric": "Gpts/s", "value": value, "unit": "Gpts/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": {"fp32": "f32", "fp16v": "f32 arithmetic, f16 u, v, w, f32 P, Q"}.get(
+                    args.storage, f"f32 arithmetic, {args.storage} wavefields"), "data": "synthetic",
                 "config": bench_config(meta, cfgd, ws),
                 "shots_per_hour": 3600.0 * 1000.0 / ms_per_step * ws,
                 "rel_l2_vs_fp64": rel,

@@ -88,7 +88,7 @@ int cuda_3dfd_tti(char *FNvel, char *FNrho, char *FNepsilon, char *FNdelta, char
 /* ------------------------------------------------------- engine API */
 
 enum a3d_physics { A3D_2ORDER = 0, A3D_ISO = 1, A3D_VTI = 2, A3D_TTI = 3 };
-enum a3d_storage { A3D_FP32 = 0, A3D_BF16 = 1, A3D_FP16 = 2, A3D_FP64 = 3 };
+enum a3d_storage { A3D_FP32 = 0, A3D_BF16 = 1, A3D_FP16 = 2, A3D_FP64 = 3, A3D_FP16V = 4 };
 
 typedef struct {
     int physics;       /* enum a3d_physics                                        */
@@ -102,8 +102,10 @@ typedef struct {
     int rec_z;         /* 2nd order: receiver depth in model cells; < 0: 1        */
     int mute;          /* zero the direct wave in the record                      */
     int storage;       /* enum a3d_storage of the wavefields: FP32, FP64 (the FP64
-                          error-reference run), or BF16 / FP16 (isotropic and VTI:
-                          2-byte fields, float arithmetic)                        */
+                          error-reference run), BF16 / FP16 (isotropic, VTI and TTI:
+                          2-byte fields, float arithmetic), or FP16V (VTI: u, v, w
+                          as float16, P, Q and the split components as float; the
+                          2-byte VTI forms whose long records stay stable)        */
     int tile_x;        /* kernel tile width along x: 8 or 16 fixes it, 0 lets the
                           autotuner choose, < 0 disables the autotuner (32x8 tiles) */
     int boundary;      /* enum a3d_boundary: A3D_BOUNDARY_PML (0, the physics' own

@@ -53,6 +53,16 @@ def test_half_storage_only_for_first_order_engines(engine_lib):
         assert rc == a3d.A3D_E_UNSUPPORTED
 
 
+def test_mixed_storage_only_for_vti(engine_lib):
+    """FP16V (float16 u, v, w, float P, Q) is built for the VTI engine only."""
+    import a3d
+    for phys in ("2o", "iso", "tti"):
+        cfg = a3d.make_config(phys, 10, 10, 10, storage=a3d.FP16V)
+        h = ctypes.c_void_p()
+        rc = a3d.lib().a3d_engine_create(ctypes.byref(h), ctypes.byref(cfg), *[a3d._fptr(None)] * 6, 0)
+        assert rc == a3d.A3D_E_UNSUPPORTED, phys
+
+
 def test_unsupported_storage_rejected(engine_lib):
     import a3d
     cfg = a3d.make_config("iso", 10, 10, 10, storage=7)

@@ -1,13 +1,16 @@
-"""GPU checks of 2-byte wavefield storage (isotropic, VTI and TTI engines).
+"""GPU checks of reduced-precision wavefield storage (isotropic, VTI and TTI engines).
 
 The wavefields u, v, w, P and the split PML components are stored as bfloat16 or
 float16 (float16 with power-of-two per-field scales); every stencil operation and
-the time integration stay float.  There is no bitwise reference for these runs:
-the record is compared with the same shot run in FP64 storage, and the tolerances
-are the stated error of each form on this case (measured on GB300: bfloat16 4.7e-2,
-float16 4.4e-3, FP32 7.7e-7), with about 2x headroom.  These bounds are regression
-guards for the 2-byte forms, not the 1e-3 precision target: no 2-byte form meets
-that target, and already this 300-step case puts float16 above it.
+the time integration stay float.  FP16V (VTI) stores u, v, w as float16 and P, Q
+and their split components as float.  There is no bitwise reference for these
+runs: the record is compared with the same shot run in FP64 storage.
+
+FP16V is held to the 1e-3 precision gate, on the 300-step case and on a 1500-step
+record of the same model (measured on GB300: 9.0e-4 and 9.3e-4).  The all-2-byte
+forms do not meet that gate; their bounds are regression guards at about 2x the
+stated error of each form on this case (measured on GB300: bfloat16 4.7e-2,
+float16 4.4e-3, FP32 7.7e-7), not the precision target.
 """
 import numpy as np
 import pytest
@@ -59,16 +62,22 @@ def test_half_storage_mutes_the_same_samples(engine_lib, fp64_record):
     assert np.all(r16[muted] == 0)
 
 
-@pytest.mark.parametrize("name,tol", [("bf16", 5e-2), ("fp16", 5e-3), ("fp32", 2e-6)])
-def test_vti_record_error_vs_fp64_within_stated_bound(engine_lib, name, tol):
-    """VTI with 2-byte storage on the 300-step case (measured: bfloat16 2.4e-2,
-    float16 2.4e-3, FP32 6.7e-7)."""
+PRECISION_GATE = 1e-3
+
+
+@pytest.mark.parametrize("name,tol,nt", [("bf16", 5e-2, NT), ("fp16", 5e-3, NT), ("fp32", 2e-6, NT),
+                                         ("fp16v", PRECISION_GATE, NT), ("fp16v", PRECISION_GATE, 1500)],
+                         ids=["bf16", "fp16", "fp32", "fp16v", "fp16v-1500"])
+def test_vti_record_error_vs_fp64_within_stated_bound(engine_lib, name, tol, nt):
+    """VTI with reduced-precision storage (measured on the 300-step case: bfloat16
+    2.4e-2, float16 2.4e-3, FP32 6.7e-7, FP16V 9.0e-4; FP16V after 1500 steps
+    9.3e-4, where bfloat16 has diverged)."""
     import a3d
     models = make_models("vti", NX, NY, NZ, seed=5)
-    code = {"bf16": a3d.BF16, "fp16": a3d.FP16, "fp32": a3d.FP32}[name]
+    code = {"bf16": a3d.BF16, "fp16": a3d.FP16, "fp32": a3d.FP32, "fp16v": a3d.FP16V}[name]
     recs = {}
     for key, st in (("ref", a3d.FP64), ("run", code)):
-        cfg = a3d.make_config("vti", NX, NY, NZ, nt=NT, dt=1e-3, fm=25.0, npml=10, storage=st)
+        cfg = a3d.make_config("vti", NX, NY, NZ, nt=nt, dt=1e-3, fm=25.0, npml=10, storage=st)
         e = a3d.Engine(cfg, models)
         try:
             recs[key] = e.run(*SHOT)

@@ -48,8 +48,8 @@ def _clear_tune():
         os.environ["A3D_TUNE"] = old
 
 
-@pytest.mark.parametrize("storage,mute", [(0, False), (0, True), (2, False), (1, True)],
-                         ids=["fp32", "fp32-mute", "fp16", "bf16-mute"])
+@pytest.mark.parametrize("storage,mute", [(0, False), (0, True), (2, False), (1, True), (4, False), (4, True)],
+                         ids=["fp32", "fp32-mute", "fp16", "bf16-mute", "fp16v", "fp16v-mute"])
 def test_sweep_records_equal_single_runs(engine_lib, models, storage, mute):
     import a3d
     ref = _singles(a3d, models, SHOTS, storage, mute)
@@ -91,6 +91,26 @@ def test_every_multishot_launch_shape(engine_lib, models):
             e.close()
         for j, r in enumerate(ref):
             assert np.array_equal(recs[j], r), f"A3D_TUNE={tune} shot {j}: {np.count_nonzero(recs[j] != r)} differ"
+
+
+def test_every_fp16v_launch_shape(engine_lib, models):
+    """float16 u, v, w with float P, Q (FP16V): every tile shape and ring depth built
+    for it, one shot and multi-shot, gives the same records."""
+    import a3d
+    ref = _singles(a3d, models, SHOTS[:2], storage=a3d.FP16V)
+    for tx, rows in ((8, 1), (16, 1), (16, 2)):
+        for depth in (0, 2):
+            os.environ["A3D_TUNE"] = f"{tx},{rows},{depth},0"
+            one = _singles(a3d, models, SHOTS[:2], storage=a3d.FP16V)
+            os.environ["A3D_TUNE"] = f"{tx},{rows},{depth},2,0,5"
+            e = a3d.Engine(_cfg(a3d, batch=2, storage=a3d.FP16V), models)
+            try:
+                recs = e.run_shots(SHOTS[:2])
+            finally:
+                e.close()
+            for j, r in enumerate(ref):
+                assert np.array_equal(one[j], r), f"one shot, {tx},{rows},{depth}: shot {j}"
+                assert np.array_equal(recs[j], r), f"sweep, {tx},{rows},{depth}: shot {j}"
 
 
 def test_run_batch_groups_shots_into_sweeps(engine_lib, models):
