@@ -564,6 +564,46 @@ def run_vti_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def round_params(models, kind):
+    """Model arrays rounded to float16 or bfloat16 (round to nearest even), as float32."""
+    out = {}
+    for k, v in models.items():
+        a = np.ascontiguousarray(v, np.float32)
+        if kind == "fp16":
+            out[k] = a.astype(np.float16).astype(np.float32)
+        else:
+            b = a.view(np.uint32).astype(np.uint64)
+            out[k] = ((b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000).astype(np.uint32).view(np.float32)
+    return out
+
+
+def run_param_rounding(args):
+    """Record error from 16-bit model parameters: the FP64 engine on the workload's
+    models rounded to float16 / bfloat16 against the FP64 engine on the exact models
+    (no timing; one JSON line per format)."""
+    import a3d
+    import build as pkg_build
+    pkg_build.build()
+    cfgd, models, shot, meta = workload(args.workload, args.nt or None)
+
+    def rec(m):
+        cfg = a3d.make_config(cfgd["physics"], cfgd["nx"], cfgd["ny"], cfgd["nz"], dx=cfgd["dx"], dy=cfgd["dy"],
+                              dz=cfgd["dz"], nt=cfgd["nt"], dt=cfgd["dt"], fm=cfgd["fm"], npml=cfgd["npml"],
+                              rec_z=cfgd.get("rec_z", -1), storage=a3d.FP64)
+        e = a3d.Engine(cfg, m)
+        try:
+            return e.run(*shot).astype(np.float64)
+        finally:
+            e.close()
+
+    r64 = rec(models)
+    n64 = np.linalg.norm(r64.ravel())
+    for kind in ("fp16", "bf16"):
+        r = rec(round_params(models, kind))
+        print(json.dumps({"workload": meta["workload"], "params": kind, "engine": "fp64",
+                          "rel_l2_vs_exact_params": float(np.linalg.norm((r - r64).ravel()) / n64)}), flush=True)
+
+
 def run_learned(args):
     """The learned absorbing rim against the PML (isotropic 256^3, d 10 m, nt 2000,
     20 Hz Ricker at the centre, depth 8): a bench step is one learned-rim shot
@@ -635,6 +675,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error check")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-legacy", action="store_true", help="skip the drop-in entry point's end-to-end timing")
+    ap.add_argument("--param-rounding", action="store_true",
+                    help="no timing: record error of 16-bit model parameters (FP64 engine)")
     ap.add_argument("--storage", default="fp32", choices=list(STORAGE),
                     help="wavefield storage (bf16 / fp16: isotropic and VTI engines; arithmetic stays fp32)")
     args = ap.parse_args()
@@ -652,6 +694,9 @@ def main():
         return
     if args.workload == "vti384batch":
         run_vti_batch(args)
+        return
+    if args.param_rounding:
+        run_param_rounding(args)
         return
     cfgd, models, shot, meta = workload(args.workload, args.nt or None)
     meta["storage"] = args.storage
