@@ -17,7 +17,7 @@ LEGACY_LIBS = {"2order": "acoustic2order.so", "1order": "acoustic1order.so",
                "vti": "acoustic1vti.so", "tti": "acoustic1tti.so"}
 
 ORDER2, ISO, VTI, TTI = 0, 1, 2, 3
-FP32, BF16, FP16, FP64, FP16V = 0, 1, 2, 3, 4  # FP16V: VTI, float16 u, v, w with float P, Q
+FP32, BF16, FP16, FP64, FP16V = 0, 1, 2, 3, 4  # FP16V: VTI / TTI, float16 u, v, w with float P, Q
 PHYSICS = {"2o": ORDER2, "iso": ISO, "vti": VTI, "tti": TTI}
 MODEL_NAMES = ("vel", "rho", "eps", "del", "theta", "phi")
 READS = {ORDER2: ("vel",), ISO: ("vel", "rho"), VTI: ("vel", "rho", "eps", "del"),

@@ -1243,7 +1243,7 @@ static int validate(const a3d_config *c) {
         return fail(A3D_E_ARG, "dx, dy, dz, dt and fm must be positive");
     if (c->storage != A3D_FP32 && c->storage != A3D_FP64 &&
         !((c->storage == A3D_BF16 || c->storage == A3D_FP16) && c->physics != A3D_2ORDER) &&
-        !(c->storage == A3D_FP16V && c->physics == A3D_VTI))
+        !(c->storage == A3D_FP16V && (c->physics == A3D_VTI || c->physics == A3D_TTI)))
         return fail(A3D_E_UNSUPPORTED, "storage type %d is not built for this engine", c->storage);
     if (c->physics == A3D_ISO && (c->wtype < 1 || c->wtype > 6))
         return fail(A3D_E_ARG, "wavelet type %d outside 1..6", c->wtype);

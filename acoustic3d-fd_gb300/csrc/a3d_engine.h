@@ -52,7 +52,7 @@ struct a3d_engine {
     // K records and K mute tables follow each other, d_shots the shots' source cells
     int nbatch = 1;
     size_t fstride = 0, fstride_p = 0;  // u, v, w / P, Q and split components (elements)
-    // A3D_FP16V: u, v, w float16 (half = 2, esz = 2), P, Q and split components float
+    // A3D_FP16V (VTI, TTI): u, v, w float16 (half = 2, esz = 2), P, Q and split components float
     bool pfloat = false;
     size_t esz_p = 4;      // bytes per element of P, Q and the split components
     int4 *d_shots = nullptr;

@@ -63,7 +63,7 @@ struct K1Launch {
     int ms;     // 1: multi-shot kernels (VTI: 4-D wavefield maps, p.shots, p.fstride, p.rstride)
     int nshot;  // multi-shot kernels: shots this launch advances (1 .. the maps' shot count)
     int sblk;   // multi-shot kernels: grid tiles per block of the tile order (Sweep::sblk)
-    int pf;     // VTI with half == 2: P, Q and split components stored as float (A3D_FP16V)
+    int pf;     // VTI / TTI with half == 2: P, Q and split components stored as float (A3D_FP16V)
 };
 
 cudaError_t launch_k1(const K1Launch &L, cudaStream_t st);
@@ -77,4 +77,5 @@ cudaError_t launch_vti(const K1Launch &L, cudaStream_t st);
 cudaError_t launch_vti_ms(const K1Launch &L, cudaStream_t st);  // L.ms (launch_vti forwards)
 cudaError_t launch_vti_pf(const K1Launch &L, cudaStream_t st);  // L.pf (launch_vti forwards)
 cudaError_t launch_tti(const K1Launch &L, cudaStream_t st);
+cudaError_t launch_tti_pf(const K1Launch &L, cudaStream_t st);  // L.pf (launch_tti forwards)
 }  // namespace a3d

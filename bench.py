@@ -78,8 +78,11 @@ STEP_BYTES_2B = {"iso": 24.0, "vti": 36.0, "tti": 40.0}
 #   velocity: P, Q (4 B) + u, v, w (2 B) + 1/rho read, u, v, w written -> 24 B; stress:
 #   u, v, w (2 B) + P, Q (4 B) + rho, vp, eps, del read, P, Q written -> 38 B; step
 #   (u, v, w) read and written at 2 B, (P, Q) at 4 B, 4 float parameters -> 44 B
-KERNEL_BYTES_MIXED = {"vti": (24.0, 38.0)}
-STEP_BYTES_MIXED = {"vti": 44.0}
+#   TTI: velocity P, Q (4 B) + u, v, w (2 B) + 4 trig floats read, u, v, w written
+#   -> 36 B; stress u, v, w (2 B) + P, Q (4 B) + vp, eps, del + 4 trig read, P, Q
+#   written -> 50 B; step (u, v, w) at 2 B, (P, Q) at 4 B, 5 float parameters -> 48 B
+KERNEL_BYTES_MIXED = {"vti": (24.0, 38.0), "tti": (36.0, 50.0)}
+STEP_BYTES_MIXED = {"vti": 44.0, "tti": 48.0}
 STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2, "fp16v": 4}
 
 
@@ -702,8 +705,8 @@ def main():
     meta["storage"] = args.storage
     if args.storage != "fp32" and cfgd["physics"] not in ("iso", "vti", "tti"):
         raise SystemExit("2-byte storage is built for the 1st-order engines only")
-    if args.storage == "fp16v" and cfgd["physics"] != "vti":
-        raise SystemExit("fp16v storage is built for the VTI engine only")
+    if args.storage == "fp16v" and cfgd["physics"] not in ("vti", "tti"):
+        raise SystemExit("fp16v storage is built for the VTI and TTI engines only")
     if args.impl == "reference":
         run_reference(args, cfgd, models, shot, meta)
         return

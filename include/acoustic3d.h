@@ -104,8 +104,9 @@ typedef struct {
     int storage;       /* enum a3d_storage of the wavefields: FP32, FP64 (the FP64
                           error-reference run), BF16 / FP16 (isotropic, VTI and TTI:
                           2-byte fields, float arithmetic), or FP16V (VTI: u, v, w
-                          as float16, P, Q and the split components as float; the
-                          2-byte VTI forms whose long records stay stable)        */
+                          as float16, P, Q and the split components as float: VTI
+                          and TTI; long records stay stable with it where the
+                          all-2-byte forms diverge)                               */
     int tile_x;        /* kernel tile width along x: 8 or 16 fixes it, 0 lets the
                           autotuner choose, < 0 disables the autotuner (32x8 tiles) */
     int boundary;      /* enum a3d_boundary: A3D_BOUNDARY_PML (0, the physics' own

@@ -53,10 +53,10 @@ def test_half_storage_only_for_first_order_engines(engine_lib):
         assert rc == a3d.A3D_E_UNSUPPORTED
 
 
-def test_mixed_storage_only_for_vti(engine_lib):
-    """FP16V (float16 u, v, w, float P, Q) is built for the VTI engine only."""
+def test_mixed_storage_only_for_vti_and_tti(engine_lib):
+    """FP16V (float16 u, v, w, float P, Q) is built for the VTI and TTI engines only."""
     import a3d
-    for phys in ("2o", "iso", "tti"):
+    for phys in ("2o", "iso"):
         cfg = a3d.make_config(phys, 10, 10, 10, storage=a3d.FP16V)
         h = ctypes.c_void_p()
         rc = a3d.lib().a3d_engine_create(ctypes.byref(h), ctypes.byref(cfg), *[a3d._fptr(None)] * 6, 0)
