@@ -33,8 +33,13 @@ struct VtiVelL {
     static constexpr size_t RB = RG::RB, B_OFF = RG::B_OFF, BAR_OFF = RG::BAR_OFF, TOTAL = RG::TOTAL;
 };
 
+// Launch bounds of the one-shot kernels name one CTA per SM as the minimum, so that
+// ptxas does not hold shapes to fewer registers with spills (measured on one GB300:
+// the 384x384x256 shot 1.8 % faster).  The multi-shot kernels keep ptxas's default
+// (0: no minimum): with the minimum their float16 sweep of 64 shots took 27.2 ms per
+// stress launch against 25.0 ms.
 template <int TX, class S, int D, int R, bool MS, bool PF>
-__global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
+__global__ void __launch_bounds__(32 * (TX / (2 * R) + 1), MS ? 0 : 1)
     vti_vel(const __grid_constant__ Maps<6> mp, S *__restrict__ u, S *__restrict__ v,
             S *__restrict__ w, const __grid_constant__ K1Params p) {
     using SP = std::conditional_t<PF, float, S>;  // P, Q storage
@@ -299,7 +304,7 @@ __device__ __forceinline__ void vti_cell(T Po, T Qo, T xx, T yy, T zz, float rv,
 }
 
 template <int TX, class S, int D, int R, bool MS, bool PF>
-__global__ void __launch_bounds__(32 * (TX / (2 * R) + 1))
+__global__ void __launch_bounds__(32 * (TX / (2 * R) + 1), MS ? 0 : 1)
     vti_stress(const __grid_constant__ Maps<15> mp, std::conditional_t<PF, float, S> *__restrict__ P,
                std::conditional_t<PF, float, S> *__restrict__ Q, const __grid_constant__ K1Params p) {
     using SP = std::conditional_t<PF, float, S>;  // P, Q and split-component storage
