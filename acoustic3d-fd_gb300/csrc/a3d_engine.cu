@@ -1288,12 +1288,20 @@ extern "C" int a3d_engine_create(a3d_engine **out, const a3d_config *cfg, const 
     if (ph == A3D_2ORDER) {
         e->npml = cfg->npml > 0 ? cfg->npml : 50;  // npd, 2O:19
         if (e->cfg.rec_z < 0) e->cfg.rec_z = 1;    // 2O:159 records at model depth 1
-        if (e->cfg.rec_z >= cfg->nz) { delete e; return fail(A3D_E_ARG, "receiver depth %d outside the model", e->cfg.rec_z); }
+        if (e->cfg.rec_z >= cfg->nz) {
+            const int rz = e->cfg.rec_z;
+            delete e;
+            return fail(A3D_E_ARG, "receiver depth %d outside the model", rz);
+        }
         e->g.set(cfg->nx, cfg->ny, cfg->nz, MM + e->npml);
     } else {
         e->learned = cfg->boundary == A3D_BOUNDARY_LEARNED;
         e->npml = cfg->npml > 0 ? cfg->npml : (e->learned ? CL_PAD : (ph == A3D_TTI ? 40 : 20));
-        if (e->npml < 6) { delete e; return fail(A3D_E_ARG, "PML width %d below 6 cells", e->npml); }
+        if (e->npml < 6) {
+            const int w = e->npml;
+            delete e;
+            return fail(A3D_E_ARG, "PML width %d below 6 cells", w);
+        }
         {
             const char *fz = getenv("A3D_FUSED");
             e->fused_ok = ph == A3D_ISO && cfg->storage == A3D_FP32 && !e->learned && !(fz && fz[0] == '0');

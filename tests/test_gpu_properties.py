@@ -17,6 +17,9 @@ runs at the 256^3, 2000-step size of the isotropic benchmark:
   0.15 ms off on a 49 ms delay).
 * The PML takes the energy out: once the wave has left the model, the pressure
   energy inside it is a tiny fraction of its peak.
+
+It also checks that the geometry checks made after the device is chosen report the
+offending value.
 """
 import numpy as np
 import pytest
@@ -114,3 +117,20 @@ def test_pml_takes_the_energy_out(engine_lib):
     # the wave crosses the 640 m model in 0.32 s; by 1.15 s it has left it (measured
     # on a GB300: 3e-10 of the peak)
     assert energy[-1] < 1e-6 * peak, energy[-1] / peak
+
+
+@pytest.mark.parametrize("physics,kw,msg", [("2o", {"rec_z": 12}, "receiver depth 12 outside the model"),
+                                            ("iso", {"npml": 4}, "PML width 4 below 6 cells")])
+def test_engine_create_rejects_bad_geometry(engine_lib, physics, kw, msg):
+    """Geometry checks that run after the device is chosen return A3D_E_ARG with the
+    offending value in the message (the engine is released before the message is
+    formatted)."""
+    import ctypes
+    import a3d
+    cfg = a3d.make_config(physics, 12, 12, 12, nt=10, **kw)
+    h = ctypes.c_void_p()
+    m = {k: np.full((12, 12, 12), 2000.0, np.float32) for k in ("vel", "rho")}
+    rc = a3d.lib().a3d_engine_create(ctypes.byref(h), ctypes.byref(cfg), a3d._fptr(m["vel"]), a3d._fptr(m["rho"]),
+                                     *[a3d._fptr(None)] * 4, 0)
+    assert rc == a3d.A3D_E_ARG
+    assert msg in a3d.last_error()
