@@ -113,11 +113,12 @@ def test_every_fp16v_launch_shape(engine_lib, models):
                 assert np.array_equal(recs[j], r), f"sweep, {tx},{rows},{depth}: shot {j}"
 
 
-def test_run_batch_groups_shots_into_sweeps(engine_lib, models):
+@pytest.mark.parametrize("storage", [0, 4], ids=["fp32", "fp16v"])
+def test_run_batch_groups_shots_into_sweeps(engine_lib, models, storage):
     import a3d
     shots = SHOTS + [(5, 5, 5)]
-    ref = _singles(a3d, models, shots)
-    recs, ms = a3d.run_batch(_cfg(a3d, batch=3), models, shots, graph=True)
+    ref = _singles(a3d, models, shots, storage)
+    recs, ms = a3d.run_batch(_cfg(a3d, batch=3, storage=storage), models, shots, graph=True)
     assert len(recs) == len(shots) and all(t > 0 for t in ms)
     for j, r in enumerate(ref):
         assert np.array_equal(recs[j], r), f"shot {j}"
