@@ -298,7 +298,9 @@ class FD:
         jt = int(np.float32(self.sg.receiver_dt) / np.float32(self.dt))
         np.ascontiguousarray(rec[::jy, ::jx, ::jt], dtype=np.float32).tofile(shotname)
 
-    def _survey_worker(self, tasks, device, graph, batch=0, chunk=4):
+    _STORAGE = {"fp32": 0, "bf16": 1, "fp16": 2, "fp16v": 4}
+
+    def _survey_worker(self, tasks, device, graph, batch=0, chunk=4, storage="fp32"):
         """Runs the tasks on one device, `chunk` shots per a3d_run_batch call (the
         multi-shot batch size for VTI when batch > 1); a writer thread writes each
         call's record files while the next call runs on the GPU (the call releases
@@ -311,6 +313,7 @@ class FD:
             return 0
         cfg = self.engine_config()
         cfg.batch = batch if (batch > 1 and self.physics == "vti") else 0
+        cfg.storage = self._STORAGE[storage]
         models = self.read_models()
         step = max(cfg.batch, chunk, 1)
         q = queue.Queue(maxsize=1)
@@ -345,23 +348,28 @@ class FD:
             raise failed[0]
         return len(tasks)
 
-    def survey(self, devices=(0,), skip_existing=False, graph=True, batch=0):
+    def survey(self, devices=(0,), skip_existing=False, graph=True, batch=0, storage="fp32"):
         """Every shot of this node through the batched entry point: one worker process
         per device, each with its round-robin share of the shots (as allocateNode splits
         nodes, readmodel.py:121-126) in a3d_run_batch calls, records written in the
         legacy layout while the next shots run.  batch > 1 (VTI): shots advance that
-        many at a time in multi-shot sweeps.  With skip_existing, complete record files
-        are kept (resume).  Snapshots are not taken on this path (run() takes them)."""
+        many at a time in multi-shot sweeps.  storage: "fp32" (the legacy entry points'
+        arithmetic), or "bf16" / "fp16" (1st-order engines) / "fp16v" (VTI, TTI) for
+        the reduced-precision wavefield forms.  With skip_existing, complete record
+        files are kept (resume).  Snapshots are not taken on this path (run() takes
+        them)."""
+        if storage not in self._STORAGE:
+            raise A3DError(f"storage {storage!r} is not one of {sorted(self._STORAGE)}")
         tasks = [t for t in self.sg.nodetask[self.nodei]
                  if not (skip_existing and os.path.exists(self.shot_name(t)) and
                          os.path.getsize(self.shot_name(t)) == self.record_bytes())]
         devices = list(devices)
         if len(devices) == 1:
-            return self._survey_worker(tasks, devices[0], graph, batch)
+            return self._survey_worker(tasks, devices[0], graph, batch, 4, storage)
         from multiprocessing import get_context
         ctx = get_context("spawn")
         with ctx.Pool(len(devices)) as pool:
-            res = [pool.apply_async(self._survey_worker, (tasks[k::len(devices)], d, graph, batch))
+            res = [pool.apply_async(self._survey_worker, (tasks[k::len(devices)], d, graph, batch, 4, storage))
                    for k, d in enumerate(devices)]
             return sum(r.get() for r in res)
 

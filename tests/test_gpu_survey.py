@@ -51,6 +51,27 @@ def test_survey_files_equal_legacy_files(engine_lib, tmp_path, eng):
     assert open(batched.shot_name(t), "rb").read() == open(legacy.shot_name(t), "rb").read()
 
 
+@pytest.mark.parametrize("eng", ["vti", "tti"])
+def test_fp16v_survey_writes_the_engine_records(engine_lib, tmp_path, eng):
+    """storage="fp16v": each record file holds the FP16V engine's record of its shot
+    in the legacy layout (VTI in multi-shot sweeps of 3, TTI one shot at a time)."""
+    import a3d
+    import readmodel as R
+    fd = _setup(R, eng, tmp_path, "fp16v")
+    assert fd.survey(devices=(0,), batch=3 if eng == "vti" else 0, storage="fp16v") == 4
+    cfg = fd.engine_config()
+    cfg.storage = a3d.FP16V
+    e = a3d.Engine(cfg, fd.read_models())
+    try:
+        for t in fd.sg.nodetask[0]:
+            rec = e.run(*t[:3])
+            want = str(tmp_path / "want.bin")
+            fd.write_record(want, rec)
+            assert open(fd.shot_name(t), "rb").read() == open(want, "rb").read(), f"shot {t[:3]}"
+    finally:
+        e.close()
+
+
 def test_vti_survey_in_multishot_sweeps(engine_lib, tmp_path):
     """batch=3 over the node's 4 shots: one sweep of 3 and one of 1, the record files
     of both written while the other runs, byte for byte the legacy entry point's."""
