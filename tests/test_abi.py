@@ -89,7 +89,7 @@ def test_multishot_sweeps_only_for_vti(engine_lib):
     """cfg.batch > 1 (multi-shot sweeps) is built for the VTI engine with FP32 or
     2-byte storage; other physics and the FP64 run refuse it before any GPU work."""
     import a3d
-    for phys, st in (("iso", a3d.FP32), ("tti", a3d.FP32), ("2o", a3d.FP32), ("vti", a3d.FP64)):
+    for phys, st in (("iso", a3d.FP32), ("tti", a3d.FP32), ("tti", a3d.FP16V), ("2o", a3d.FP32), ("vti", a3d.FP64)):
         cfg = a3d.make_config(phys, 10, 10, 10, storage=st, batch=4)
         h = ctypes.c_void_p()
         rc = a3d.lib().a3d_engine_create(ctypes.byref(h), ctypes.byref(cfg), *[a3d._fptr(None)] * 6, 0)
