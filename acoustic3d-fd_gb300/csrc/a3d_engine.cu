@@ -1510,10 +1510,12 @@ extern "C" int a3d_engine_describe(a3d_engine *e, char *buf, size_t n) {
     }
     snprintf(buf, n,
              "{\"grid\": [%d, %d, %d], \"ldz\": %d, \"pad\": %d, \"device_bytes\": %zu, \"fused\": %d, "
+             "\"sig_v_log2\": %d, \"sig_p_log2\": %d, "
              "\"kernels\": [{\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"rot\": %d, \"sblk\": %d, "
              "\"ms\": %.4f}, {\"tile_x\": %d, \"rows\": %d, \"depth\": %d, \"plan\": %d, \"rot\": %d, \"sblk\": %d, "
              "\"ms\": %.4f}]}",
-             e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, (int)e->fused, e->tune[0].tx, e->tune[0].rows,
+             e->g.nnz, e->g.nnx, e->g.nny, e->g.ldz, e->g.pad, e->dev_bytes, (int)e->fused, ilogbf(e->sig_v),
+             ilogbf(e->sig_p), e->tune[0].tx, e->tune[0].rows,
              e->tune[0].depth, e->tune[0].mode, e->tune[0].rot, e->tune[0].sblk, e->tune[0].ms, e->tune[1].tx,
              e->tune[1].rows, e->tune[1].depth, e->tune[1].mode, e->tune[1].rot, e->tune[1].sblk, e->tune[1].ms);
     return A3D_OK;

@@ -216,8 +216,10 @@ int a3d_run_batch(const a3d_problem *pb, const a3d_shot *shots, int nshot, const
 int a3d_engine_set_profiling(a3d_engine *e, int on);
 int a3d_engine_kernel_times(const a3d_engine *e, double *ms, long long *launches);
 
-/* JSON description of the engine (grid, layout, bytes held, the autotuned launch
- * configuration of each kernel kind); runs the autotuner if it has not run. */
+/* JSON description of the engine (grid, layout, bytes held, the power-of-two
+ * scales of float16 storage as log2 — sig_v_log2 for u, v, w, sig_p_log2 for P, Q,
+ * 0 for other storage — and the autotuned launch configuration of each kernel
+ * kind); runs the autotuner if it has not run. */
 int a3d_engine_describe(a3d_engine *e, char *buf, size_t n);
 
 /* Message of the last failure on the calling thread ("" if none). */

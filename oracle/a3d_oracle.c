@@ -22,6 +22,7 @@
 #include "a3d_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -65,6 +66,36 @@ static inline float mul_df(float v, float fhi, float flo) {
     float err = fmaf(fhi, v, -p);
     return p + fmaf(flo, v, err);
 }
+
+/* x rounded to the nearest float16 value (ties to even, float16 subnormals,
+ * overflow to infinity), returned as float: IEEE 754 binary16 rounding restated
+ * on the float's bits, the conversion the CUDA engine's float16 stores make. */
+static inline float round_f16(float x) {
+    uint32_t b;
+    memcpy(&b, &x, 4);
+    const uint32_t sign = b & 0x80000000u, a = b & 0x7fffffffu;
+    if (a > 0x7f800000u) return x;                       /* NaN */
+    if (a >= 0x477ff000u) {                              /* |x| >= 65520: infinity */
+        const uint32_t r = sign | 0x7f800000u;
+        float f;
+        memcpy(&f, &r, 4);
+        return f;
+    }
+    if (a >= 0x38800000u) {                              /* normal float16: 10 fraction bits */
+        const uint32_t r = ((a + 0xfffu + ((a >> 13) & 1u)) & ~0x1fffu) | sign;
+        float f;
+        memcpy(&f, &r, 4);
+        return f;
+    }
+    const float q = nearbyintf(fabsf(x) * 16777216.0f) / 16777216.0f;  /* multiples of 2^-24 */
+    return sign ? -q : q;
+}
+
+float a3d_oracle_round_f16(float x) { return round_f16(x); }
+
+/* a velocity as the FP16V engine stores it: float16 of scale * v, divided back
+ * (scale and 1/scale are powers of two, so both products are exact) */
+static inline float store_f16s(float v, float scale, float inv) { return round_f16(v * scale) * inv; }
 
 /* ------------------------------------------------------------------------- */
 /* setup pieces                                                               */
@@ -228,6 +259,8 @@ static double sv_taper(int rx, int ry, int rz) {
 #include "a3d_oracle_loops.inc"
 #undef REAL
 #undef RFMA
+#undef RSQRT
+#undef VSTORE
 #undef SUF
 #undef IS_F32
 
@@ -238,5 +271,7 @@ static double sv_taper(int rx, int ry, int rz) {
 #include "a3d_oracle_loops.inc"
 #undef REAL
 #undef RFMA
+#undef RSQRT
+#undef VSTORE
 #undef SUF
 #undef IS_F32

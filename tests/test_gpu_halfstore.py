@@ -177,3 +177,28 @@ def test_fp16v_snapshots_follow_the_fp32_run(engine_lib, physics):
         err16 = rel_l2(snaps16[k], snaps32[k])
         print(f"{physics} snapshot {k}: FP16V {err:.3e}, float16 {err16:.3e}")
         assert err <= 2e-2 and err < err16, f"{physics} snapshot {k}: FP16V {err:.3e}, float16 {err16:.3e}"
+
+
+@pytest.mark.parametrize("physics,mute", [("vti", False), ("tti", False), ("vti", True)],
+                         ids=["vti", "tti", "vti-mute"])
+def test_fp16v_bitwise_vs_oracle_emulation(engine_lib, physics, mute):
+    """FP16V records equal, bit for bit, the float oracle's engine form with u, v, w
+    rounded after every update to the float16 value of 2^k u, k the engine's
+    velocity scale (its scales are powers of two, so the scaled float16 storage is
+    the FP32 arithmetic times powers of two, rounded where the engine stores)."""
+    import a3d
+    import oracle as O
+    models = make_models(physics, NX, NY, NZ, seed=5)
+    nt = NT
+    cfg = a3d.make_config(physics, NX, NY, NZ, nt=nt, dt=1e-3, fm=25.0, npml=10, storage=a3d.FP16V, mute=mute)
+    e = a3d.Engine(cfg, models)
+    try:
+        rec = e.run(*SHOT)
+        k = e.describe()["sig_v_log2"]
+    finally:
+        e.close()
+    s = O.Shot(NX, NY, NZ, sx=SHOT[0], sy=SHOT[1], sz=SHOT[2], nt=nt, dt=1e-3, fm=25.0, npml=10, mute=mute, form=1,
+               store=4, sig_v_log2=k)
+    ref, _ = O.run(physics, s, models, "f32")
+    assert np.abs(ref).max() > 0
+    assert np.array_equal(rec, ref), f"{int(np.count_nonzero(rec != ref))} samples differ (k = {k})"
