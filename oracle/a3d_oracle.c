@@ -93,6 +93,20 @@ static inline float round_f16(float x) {
 
 float a3d_oracle_round_f16(float x) { return round_f16(x); }
 
+/* x rounded to the nearest bfloat16 value (ties to even; overflow to infinity),
+ * returned as float: the conversion the CUDA engine's bfloat16 stores make. */
+static inline float round_bf16(float x) {
+    uint32_t b;
+    memcpy(&b, &x, 4);
+    if ((b & 0x7fffffffu) > 0x7f800000u) return x;      /* NaN */
+    b = (b + 0x7fffu + ((b >> 16) & 1u)) & 0xffff0000u;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+float a3d_oracle_round_bf16(float x) { return round_bf16(x); }
+
 /* a velocity as the FP16V engine stores it: float16 of scale * v, divided back
  * (scale and 1/scale are powers of two, so both products are exact) */
 static inline float store_f16s(float v, float scale, float inv) { return round_f16(v * scale) * inv; }
@@ -259,8 +273,6 @@ static double sv_taper(int rx, int ry, int rz) {
 #include "a3d_oracle_loops.inc"
 #undef REAL
 #undef RFMA
-#undef RSQRT
-#undef VSTORE
 #undef SUF
 #undef IS_F32
 
@@ -271,7 +283,5 @@ static double sv_taper(int rx, int ry, int rz) {
 #include "a3d_oracle_loops.inc"
 #undef REAL
 #undef RFMA
-#undef RSQRT
-#undef VSTORE
 #undef SUF
 #undef IS_F32

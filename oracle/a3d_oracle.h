@@ -49,11 +49,14 @@ typedef struct {
     int snap_skip0;        /* 1: never take a snapshot at it == 0               */
     int form;              /* 0 literal, 1 engine                               */
     int threads;           /* OpenMP threads (0 = runtime default)              */
-    int store;             /* float oracle, engine form, VTI / TTI: 0 float
-                              wavefields; 4 u, v, w rounded after every update to
-                              the float16 value of 2^sig_v_log2 * u (the CUDA
-                              engine's FP16V storage), P, Q float                */
-    int sig_v_log2;        /* the velocity scale of store 4 (the engine's)      */
+    int store;             /* float oracle, engine form, 1st-order engines: the
+                              CUDA engine's wavefield storage emulated — 0 float;
+                              1 bfloat16 (every field); 2 float16 of 2^k x (every
+                              field: k = sig_v_log2 for u, v, w, sig_p_log2 for P,
+                              Q and split components); 4 (VTI, TTI) float16 u, v,
+                              w at 2^sig_v_log2, P, Q float (FP16V)               */
+    int sig_v_log2;        /* the engine's scales of store 2 / 4 (log2)         */
+    int sig_p_log2;
 } a3d_oracle_cfg;
 
 /* Return 0 on success, negative on bad arguments / allocation failure. */
@@ -80,6 +83,7 @@ int a3d_oracle_tti_f64(const a3d_oracle_cfg *c, const float *vel, const float *e
 /* Setup pieces, exported so tests can check them on their own. */
 float a3d_oracle_ricker2o(int it, float dt, float fm);               /* Toa_3dfd_cuda.cu:34-43 */
 float a3d_oracle_round_f16(float x);  /* x rounded to float16 (ties to even), as float  */
+float a3d_oracle_round_bf16(float x); /* x rounded to bfloat16 (ties to even), as float */
 float a3d_oracle_wavelet(int wtype, float t, float fm);              /* ..iso..:52-87          */
 float a3d_oracle_d0(const float *vp_padded, int nnx, int nny, int nnz, int npml,
                     float dx, float dy, float dz);                   /* ..iso..:193-195        */

@@ -38,7 +38,7 @@ class OracleCfg(ctypes.Structure):
         ("wtype", ctypes.c_int), ("npml", ctypes.c_int), ("rec_z", ctypes.c_int),
         ("mute", ctypes.c_int), ("snap_every", ctypes.c_int), ("snap_skip0", ctypes.c_int),
         ("form", ctypes.c_int), ("threads", ctypes.c_int),
-        ("store", ctypes.c_int), ("sig_v_log2", ctypes.c_int),
+        ("store", ctypes.c_int), ("sig_v_log2", ctypes.c_int), ("sig_p_log2", ctypes.c_int),
     ]
 
 
@@ -65,8 +65,9 @@ class Shot:
     snap_skip0: bool = False
     form: int = 0
     threads: int = 0
-    store: int = 0          # 4: FP16V storage emulated (float oracle, engine form, VTI / TTI)
-    sig_v_log2: int = 0     # its velocity scale, log2 (the engine reports it)
+    store: int = 0          # engine storage emulated (float oracle, engine form): 1 bf16, 2 fp16, 4 FP16V
+    sig_v_log2: int = 0     # float16 scales, log2 (the engine reports them)
+    sig_p_log2: int = 0
     extra: dict = field(default_factory=dict)
 
     def cfg(self) -> OracleCfg:
@@ -74,7 +75,7 @@ class Shot:
                          self.sx, self.sy, self.sz, self.nt, self.dt, self.fm,
                          self.wtype, self.npml, self.rec_z, int(self.mute),
                          self.snap_every, int(self.snap_skip0), self.form, self.threads, self.store,
-                         self.sig_v_log2)
+                         self.sig_v_log2, self.sig_p_log2)
 
     def n_snaps(self) -> int:
         if self.snap_every <= 0:
@@ -112,6 +113,8 @@ def lib() -> ctypes.CDLL:
         L.a3d_oracle_wavelet.restype = ctypes.c_float
         L.a3d_oracle_round_f16.argtypes = [ctypes.c_float]
         L.a3d_oracle_round_f16.restype = ctypes.c_float
+        L.a3d_oracle_round_bf16.argtypes = [ctypes.c_float]
+        L.a3d_oracle_round_bf16.restype = ctypes.c_float
         L.a3d_oracle_d0.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.a3d_oracle_d0.restype = ctypes.c_float

@@ -179,26 +179,37 @@ def test_fp16v_snapshots_follow_the_fp32_run(engine_lib, physics):
         assert err <= 2e-2 and err < err16, f"{physics} snapshot {k}: FP16V {err:.3e}, float16 {err16:.3e}"
 
 
-@pytest.mark.parametrize("physics,mute", [("vti", False), ("tti", False), ("vti", True)],
-                         ids=["vti", "tti", "vti-mute"])
-def test_fp16v_bitwise_vs_oracle_emulation(engine_lib, physics, mute):
-    """FP16V records equal, bit for bit, the float oracle's engine form with u, v, w
-    rounded after every update to the float16 value of 2^k u, k the engine's
-    velocity scale (its scales are powers of two, so the scaled float16 storage is
-    the FP32 arithmetic times powers of two, rounded where the engine stores)."""
+EMU_CASES = [("vti", "fp16v", False), ("tti", "fp16v", False), ("vti", "fp16v", True), ("iso", "bf16", False),
+             ("iso", "fp16", False), ("iso", "fp16", True), ("vti", "bf16", False), ("vti", "fp16", False),
+             ("tti", "bf16", False), ("tti", "fp16", False)]
+
+
+@pytest.mark.parametrize("physics,storage,mute", EMU_CASES,
+                         ids=[f"{p}-{s}" + ("-mute" if m else "") for p, s, m in EMU_CASES])
+def test_reduced_storage_bitwise_vs_oracle_emulation(engine_lib, physics, storage, mute):
+    """Reduced-precision records equal, bit for bit, the float oracle's engine form
+    with the engine's storage emulated (oracle `store`): every stored field rounded
+    where the engine stores it — bfloat16, float16 of 2^k x with the engine's scales
+    k, or (FP16V) float16 u, v, w with float P, Q — the velocity sweep's view of the
+    injected source rounded as the engine rounds it, and the record sampled before
+    the pressure is rounded; snapshots (the stored pressure) too.  The scales are
+    powers of two, so scaled storage is the FP32 arithmetic times exact powers of
+    two, rounded where the engine stores."""
     import a3d
     import oracle as O
     models = make_models(physics, NX, NY, NZ, seed=5)
-    nt = NT
-    cfg = a3d.make_config(physics, NX, NY, NZ, nt=nt, dt=1e-3, fm=25.0, npml=10, storage=a3d.FP16V, mute=mute)
+    code = {"bf16": a3d.BF16, "fp16": a3d.FP16, "fp16v": a3d.FP16V}[storage]
+    cfg = a3d.make_config(physics, NX, NY, NZ, nt=NT, dt=1e-3, fm=25.0, npml=10, storage=code, mute=mute)
     e = a3d.Engine(cfg, models)
     try:
-        rec = e.run(*SHOT)
-        k = e.describe()["sig_v_log2"]
+        rec, snaps = e.run(*SHOT, snap_every=100, snap_skip0=True)
+        d = e.describe()
     finally:
         e.close()
-    s = O.Shot(NX, NY, NZ, sx=SHOT[0], sy=SHOT[1], sz=SHOT[2], nt=nt, dt=1e-3, fm=25.0, npml=10, mute=mute, form=1,
-               store=4, sig_v_log2=k)
-    ref, _ = O.run(physics, s, models, "f32")
+    s = O.Shot(NX, NY, NZ, sx=SHOT[0], sy=SHOT[1], sz=SHOT[2], nt=NT, dt=1e-3, fm=25.0, npml=10, mute=mute, form=1,
+               snap_every=100, snap_skip0=True, store=code, sig_v_log2=d["sig_v_log2"], sig_p_log2=d["sig_p_log2"])
+    ref, rsn = O.run(physics, s, models, "f32", snaps=True)
     assert np.abs(ref).max() > 0
-    assert np.array_equal(rec, ref), f"{int(np.count_nonzero(rec != ref))} samples differ (k = {k})"
+    assert np.array_equal(rec, ref), f"{int(np.count_nonzero(rec != ref))} samples differ (scales {d['sig_v_log2']}, " \
+                                     f"{d['sig_p_log2']})"
+    assert snaps.shape == rsn.shape and np.array_equal(snaps, rsn), "snapshots differ"

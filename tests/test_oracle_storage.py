@@ -1,13 +1,14 @@
-"""The oracle's emulation of the engines' FP16V storage (CPU; test infrastructure).
+"""The oracle's emulation of the engines' reduced-precision storage (CPU; test
+infrastructure).
 
-FP16V keeps u, v, w as float16 values of 2^k u (k the engine's velocity scale) and
-P, Q as float; since the scales are powers of two, the engine's arithmetic is the
-FP32 engine form times powers of two, rounded where the engine stores.  The float
-oracle emulates that with `store = 4`: after every velocity update it rounds u, v,
-w to the float16 grid of the scaled value.  Here: the rounding against numpy's IEEE
-binary16 conversion (ties to even, subnormals, overflow), and the emulated records
-against the double oracle.  tests/test_gpu_halfstore.py compares the CUDA FP16V
-records with this emulation bit for bit.
+The engines store wavefields as bfloat16, as float16 of 2^k x (k the engine's
+power-of-two scales), or (FP16V) u, v, w as scaled float16 with P, Q float; since
+the scales are powers of two, the engine's arithmetic is the FP32 engine form times
+powers of two, rounded where the engine stores.  The float oracle emulates that
+with `store` = 1, 2, 4.  Here: the roundings against IEEE binary16 (numpy's
+conversion: ties to even, subnormals, overflow) and known bfloat16 values, and the
+emulated records against the double oracle.  tests/test_gpu_halfstore.py compares
+the CUDA records with this emulation bit for bit.
 """
 import numpy as np
 import pytest
@@ -54,3 +55,35 @@ def test_fp16v_emulation_error_vs_double_oracle(physics):
     assert not np.array_equal(r16, r32)
     err16, err32 = rel_l2(r16, r64), rel_l2(r32, r64)
     assert err32 < 2e-6 and err16 <= 1e-3 and err16 > 10 * err32, (err16, err32)
+
+
+def test_round_bf16_known_values():
+    import oracle as O
+    L = O.lib()
+    cases = [(1.0 + 2.0 ** -8, 1.0), (1.0 + 3 * 2.0 ** -8, 1.0 + 2.0 ** -6), (1.0 + 2.0 ** -9, 1.0),
+             (-(1.0 + 2.0 ** -7 + 2.0 ** -9), -(1.0 + 2.0 ** -7)), (3.0e38, 3.0040553e38), (0.0, 0.0), (2.5, 2.5)]
+    for x, want in cases:
+        got = L.a3d_oracle_round_bf16(float(np.float32(x)))
+        assert abs(got - want) <= abs(want) * 1e-4, (x, got, want)
+    assert np.isinf(L.a3d_oracle_round_bf16(float(np.finfo(np.float32).max)))
+
+
+@pytest.mark.parametrize("physics", ["iso", "vti", "tti"])
+def test_two_byte_emulation_errors_order(physics):
+    """Emulated bfloat16 and float16 storage: both differ from the float engine form;
+    float16 (11-bit significand) lies closer to the double oracle than bfloat16 (8)."""
+    import oracle as O
+    nx, ny, nz, nt = 24, 22, 20, 150
+    m = make_models(physics, nx, ny, nz, seed=9)
+    kw = dict(sx=11, sy=10, sz=4, nt=nt, dt=1e-3, fm=25.0, npml=8, form=1)
+    r64, _ = O.run(physics, O.Shot(nx, ny, nz, **kw), m, "f64")
+    r32, _ = O.run(physics, O.Shot(nx, ny, nz, **kw), m, "f32")
+    kv = 20 if physics == "tti" else (21 if physics == "iso" else 31)
+    kp = -3 if physics == "iso" else 7
+    err = {}
+    for st in (1, 2):
+        r, _ = O.run(physics, O.Shot(nx, ny, nz, store=st, sig_v_log2=kv, sig_p_log2=kp, **kw), m, "f32")
+        assert not np.array_equal(r, r32)
+        err[st] = rel_l2(r, r64)
+    assert rel_l2(r32, r64) < err[2] < err[1] < 0.2, err
+
