@@ -3,10 +3,10 @@
 The wavefields u, v, w, P and the split PML components are stored as bfloat16 or
 float16 (float16 with power-of-two per-field scales); every stencil operation and
 the time integration stay float.  FP16V (VTI, TTI) stores u, v, w as float16 and
-P, Q and their split components as float.  There is no bitwise reference for these
-runs: the record is compared with the same shot run in FP64 storage, and with the
-float oracle's emulation of the storage bit for bit
-(test_reduced_storage_bitwise_vs_oracle_emulation).
+P, Q and their split components as float.  Each form's record is compared bit for
+bit with the float oracle's emulation of its storage
+(test_reduced_storage_bitwise_vs_oracle_emulation), and its error with the same
+shot run in FP64 storage.
 
 FP16V is held to the 1e-3 precision gate, on the 300-step case and on a 1500-step
 record of the same model (measured on GB300: VTI 9.0e-4 and 9.3e-4, TTI 9.2e-4 and
