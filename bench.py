@@ -792,7 +792,11 @@ def main():
     if desc.get("fused"):
         kname = "iso_step"
     tr = traffic_per_launch(meta["workload"] + ("" if args.storage == "fp32" else "_" + args.storage))
-    traffic = tr.get(kname) if isinstance(tr, dict) else None
+    # DRAM bytes of the launch shape the tuner picked ("kernel@<tile x>x<rows>"), else
+    # of the kernel's profiled shape
+    kd = tuning[min(dom, len(tuning) - 1)] if tuning else {}
+    shape_key = "%s@%dx%d" % (kname, kd.get("tile_x", 0), kd.get("rows", 0))
+    traffic = (tr.get(shape_key, tr.get(kname)) if isinstance(tr, dict) else None)
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
                 "peak_source": peak_kind, "bytes_per_cell": kb[dom],
