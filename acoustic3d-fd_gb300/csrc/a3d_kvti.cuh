@@ -1,6 +1,7 @@
 // a3d_kvti.cuh — 1st-order pseudo-acoustic VTI engine (u, v, w, P, Q; rho, eps, delta):
-// the kernel templates, instantiated by a3d_kvti.cu (one shot per launch) and
-// a3d_kvti_ms.cu (multi-shot sweeps), which compile in parallel.
+// the kernel templates, instantiated by a3d_kvti.cu (one shot per launch),
+// a3d_kvti_ms.cu (multi-shot sweeps) and a3d_kvti_pf.cu (float16 u, v, w with float
+// P, Q: PF = true), which compile in parallel.
 //
 //   vti_vel:    u,v <- D+P (x, y);  w <- D+_z Q;  / rho          (..vti..:91-128)
 //               the Ricker monopole enters the sweep's views of P and Q only
