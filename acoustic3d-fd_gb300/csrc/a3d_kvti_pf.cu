@@ -10,7 +10,8 @@ template <bool MS>
 static cudaError_t launch_vti_pf_t(const K1Launch &L, cudaStream_t st) {
     if (L.depth == 1 || L.rows == 4 || (L.tx == 8 && L.rows != 1)) return cudaErrorInvalidConfiguration;
     if (L.tx == 8)
-        return L.depth ? launch_vti_s<8, __half, 2, 1, MS, true>(L, st) : launch_vti_s<8, __half, 0, 1, MS, true>(L, st);
+        return L.depth ? launch_vti_s<8, __half, 2, 1, MS, true>(L, st)
+                       : launch_vti_s<8, __half, 0, 1, MS, true>(L, st);
     if (L.rows == 1)
         return L.depth ? launch_vti_s<16, __half, 2, 1, MS, true>(L, st)
                        : launch_vti_s<16, __half, 0, 1, MS, true>(L, st);
