@@ -107,6 +107,20 @@ static inline float round_bf16(float x) {
 
 float a3d_oracle_round_bf16(float x) { return round_bf16(x); }
 
+/* x rounded to a 24-bit float: float's sign and exponent, 15 fraction bits (the low
+ * 8 rounded off, ties to even; overflow to infinity) */
+static inline float round_f24(float x) {
+    uint32_t b;
+    memcpy(&b, &x, 4);
+    if ((b & 0x7fffffffu) > 0x7f800000u) return x;      /* NaN */
+    b = (b + 0x7fu + ((b >> 8) & 1u)) & ~0xffu;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+float a3d_oracle_round_f24(float x) { return round_f24(x); }
+
 /* a velocity as the FP16V engine stores it: float16 of scale * v, divided back
  * (scale and 1/scale are powers of two, so both products are exact) */
 static inline float store_f16s(float v, float scale, float inv) { return round_f16(v * scale) * inv; }

@@ -54,7 +54,10 @@ typedef struct {
                               1 bfloat16 (every field); 2 float16 of 2^k x (every
                               field: k = sig_v_log2 for u, v, w, sig_p_log2 for P,
                               Q and split components); 4 (VTI, TTI) float16 u, v,
-                              w at 2^sig_v_log2, P, Q float (FP16V)               */
+                              w at 2^sig_v_log2, P, Q float (FP16V).  Formats no
+                              engine stores yet, for measuring them: 5 every field
+                              a 24-bit float (float with the low 8 significand bits
+                              rounded off); 6 u, v, w 24-bit, P, Q float          */
     int sig_v_log2;        /* the engine's scales of store 2 / 4 (log2)         */
     int sig_p_log2;
 } a3d_oracle_cfg;
@@ -84,6 +87,7 @@ int a3d_oracle_tti_f64(const a3d_oracle_cfg *c, const float *vel, const float *e
 float a3d_oracle_ricker2o(int it, float dt, float fm);               /* Toa_3dfd_cuda.cu:34-43 */
 float a3d_oracle_round_f16(float x);  /* x rounded to float16 (ties to even), as float  */
 float a3d_oracle_round_bf16(float x); /* x rounded to bfloat16 (ties to even), as float */
+float a3d_oracle_round_f24(float x);  /* x rounded to a 24-bit float (ties to even)     */
 float a3d_oracle_wavelet(int wtype, float t, float fm);              /* ..iso..:52-87          */
 float a3d_oracle_d0(const float *vp_padded, int nnx, int nny, int nnz, int npml,
                     float dx, float dy, float dz);                   /* ..iso..:193-195        */

@@ -65,7 +65,8 @@ class Shot:
     snap_skip0: bool = False
     form: int = 0
     threads: int = 0
-    store: int = 0          # engine storage emulated (float oracle, engine form): 1 bf16, 2 fp16, 4 FP16V
+    store: int = 0          # storage emulated (float oracle, engine form): 1 bf16, 2 fp16, 4 FP16V; 5 / 6 24-bit
+                            # floats (every field / u, v, w only), a format no engine stores yet
     sig_v_log2: int = 0     # float16 scales, log2 (the engine reports them)
     sig_p_log2: int = 0
     extra: dict = field(default_factory=dict)
@@ -115,6 +116,8 @@ def lib() -> ctypes.CDLL:
         L.a3d_oracle_round_f16.restype = ctypes.c_float
         L.a3d_oracle_round_bf16.argtypes = [ctypes.c_float]
         L.a3d_oracle_round_bf16.restype = ctypes.c_float
+        L.a3d_oracle_round_f24.argtypes = [ctypes.c_float]
+        L.a3d_oracle_round_f24.restype = ctypes.c_float
         L.a3d_oracle_d0.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.a3d_oracle_d0.restype = ctypes.c_float

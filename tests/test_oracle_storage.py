@@ -87,3 +87,31 @@ def test_two_byte_emulation_errors_order(physics):
         err[st] = rel_l2(r, r64)
     assert rel_l2(r32, r64) < err[2] < err[1] < 0.2, err
 
+
+
+def test_round_f24_known_values():
+    import oracle as O
+    L = O.lib()
+    one = np.float32(1.0)
+    cases = [(1.0 + 2.0 ** -16, 1.0), (1.0 + 3 * 2.0 ** -16, 1.0 + 2.0 ** -14), (1.0 + 2.0 ** -15, 1.0 + 2.0 ** -15),
+             (-(2.0 + 2.0 ** -15), -2.0), (0.0, 0.0), (float(one), 1.0)]
+    for x, want in cases:
+        got = L.a3d_oracle_round_f24(float(np.float32(x)))
+        assert got == np.float32(want), (x, got, want)
+    assert np.isinf(L.a3d_oracle_round_f24(float(np.finfo(np.float32).max)))
+
+
+def test_f24_emulation_error_vs_double_oracle():
+    """The 24-bit formats (no engine stores them yet): velocities only (store 6) and
+    every field (store 5) lie far inside the precision gate on a small VTI case, and
+    below the float16 forms' errors."""
+    import oracle as O
+    nx, ny, nz, nt = 24, 22, 20, 150
+    m = make_models("vti", nx, ny, nz, seed=9)
+    kw = dict(sx=11, sy=10, sz=4, nt=nt, dt=1e-3, fm=25.0, npml=8, form=1)
+    r64, _ = O.run("vti", O.Shot(nx, ny, nz, **kw), m, "f64")
+    err = {}
+    for st in (2, 4, 5, 6):
+        r, _ = O.run("vti", O.Shot(nx, ny, nz, store=st, sig_v_log2=31, sig_p_log2=7, **kw), m, "f32")
+        err[st] = rel_l2(r, r64)
+    assert err[6] < err[5] < 1e-3 and err[6] < err[4] and err[5] < err[2], err
